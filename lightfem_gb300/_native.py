@@ -1,0 +1,288 @@
+"""ctypes binding of liblfgpu.so (the C ABI declared in include/lfgpu.h).
+
+Loading fails loudly: there is no CPU fallback anywhere in this package.  If the
+library is missing, build it with ``lightfem_gb300.build.build()``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_void_p
+
+import numpy as np
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "liblfgpu.so")
+
+# enums of include/lfgpu.h
+OK = 0
+ERR_ARGUMENT, ERR_CUDA, ERR_STATE, ERR_JACOBIAN, ERR_EDGE, ERR_MECHANISM = 1, 2, 3, 4, 5, 6
+ERR_NOT_SPD, ERR_RHO_INITIAL, ERR_RHO, ERR_NONFINITE_DIAG, ERR_TIMEOUT, ERR_NOMEM, ERR_UNSUPPORTED = (
+    7, 8, 9, 10, 11, 12, 13)
+ASSEMBLY = {"coloring": 0, "atomic": 1}
+STORAGE = {"csr": 0, "bsr": 1}
+PRECOND = {"jacobi": 0, "block": 1, "ic0": 2}
+PRECISION = {"fp64": 0, "mixed": 1}
+REFINEMENT = {"reliable": 0, "restart": 1}
+K_FULL, K_CONSTRAINED, F_FULL, F_CONSTRAINED, U, R = range(6)
+
+
+class SolveOptions(ctypes.Structure):
+    _fields_ = [("tolerance", c_double), ("max_iterations", c_int64), ("storage", c_int32),
+                ("preconditioner", c_int32), ("precision", c_int32), ("refinement", c_int32),
+                ("inner_reduction", c_double), ("max_refinements", c_int64)]
+
+
+class Report(ctypes.Structure):
+    _fields_ = [("converged", c_int32), ("status", c_int32), ("iterations", c_int64), ("refinements", c_int64),
+                ("initial_residual", c_double), ("final_residual", c_double), ("true_residual", c_double),
+                ("solve_ms", c_double), ("matvec_ms", c_double), ("matvec_calls", c_int64),
+                ("matrix_bytes_per_matvec", c_int64), ("storage_convert_ms", c_double),
+                ("preconditioner_setup_ms", c_double), ("preconditioner_apply_ms", c_double),
+                ("subdomains", c_int64), ("capture_ratio", c_double), ("degenerate_subdomains", c_int64),
+                ("ic0_breakdowns", c_int64), ("ic0_levels", c_int64), ("fallback_fp64", c_int64)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class Timings(ctypes.Structure):
+    _fields_ = [("pattern_ms", c_double), ("assembly_ms", c_double), ("boundary_ms", c_double),
+                ("reactions_ms", c_double), ("coloring_count", c_int64)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class GpuError(RuntimeError):
+    """A non-zero status from liblfgpu; ``code`` is the lfgpu_status value."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+_lib = None
+
+_SIGNATURES = {
+    "lfgpu_create": (c_int, [c_int, POINTER(c_void_p)]),
+    "lfgpu_destroy": (c_int, [c_void_p]),
+    "lfgpu_last_error": (c_char_p, [c_void_p]),
+    "lfgpu_version": (c_char_p, []),
+    "lfgpu_set_mesh": (c_int, [c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_void_p, c_int64, c_void_p,
+                               c_void_p, c_void_p, c_int32]),
+    "lfgpu_set_young": (c_int, [c_void_p, c_void_p]),
+    "lfgpu_set_pattern": (c_int, [c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "lfgpu_build_pattern": (c_int, [c_void_p]),
+    "lfgpu_pattern_info": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
+    "lfgpu_download_pattern": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "lfgpu_set_loads": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
+                                c_void_p, c_void_p, c_void_p, c_void_p]),
+    "lfgpu_set_constraints": (c_int, [c_void_p, c_int64, c_void_p, c_void_p]),
+    "lfgpu_assemble": (c_int, [c_void_p, c_int32]),
+    "lfgpu_apply_dirichlet": (c_int, [c_void_p]),
+    "lfgpu_solve": (c_int, [c_void_p, POINTER(SolveOptions), c_void_p, POINTER(Report)]),
+    "lfgpu_reactions": (c_int, [c_void_p, c_void_p]),
+    "lfgpu_download": (c_int, [c_void_p, c_int32, c_void_p]),
+    "lfgpu_timings_get": (c_int, [c_void_p, POINTER(Timings)]),
+    "lfgpu_spmv": (c_int, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, POINTER(c_double)]),
+    "lfgpu_adjoint": (c_int, [c_void_p, c_void_p, POINTER(SolveOptions), c_void_p, POINTER(Report)]),
+    "lfgpu_host_rcm": (c_int, [c_int64, c_void_p, c_int64, c_void_p, c_void_p]),
+}
+
+EXPORTED = tuple(_SIGNATURES)
+
+
+def library() -> ctypes.CDLL:
+    """Load liblfgpu.so once; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with lightfem_gb300.build.build() "
+                              "(the CUDA path has no CPU fallback)")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data
+
+
+def _arr(a, dtype) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a), dtype=dtype)
+
+
+def host_rcm(node_ids: np.ndarray, element_node_ids: np.ndarray) -> np.ndarray:
+    """reverse_cuthill_mckee (src/reordering.cpp:11-62) on node IDs -> new ID order."""
+    ids = _arr(node_ids, np.int64)
+    en = _arr(element_node_ids, np.int64).reshape(-1)
+    out = np.empty(ids.shape[0], np.int64)
+    rc = library().lfgpu_host_rcm(ids.shape[0], _ptr(ids), en.shape[0] // 4, _ptr(en), _ptr(out))
+    if rc != OK:
+        raise GpuError(rc, "RCM ordering failed: element references an unknown node ID")
+    return out
+
+
+class Context:
+    """One liblfgpu handle: a CUDA stream and the device copy of one model."""
+
+    def __init__(self, device: int = 0):
+        self._lib = library()
+        h = c_void_p()
+        rc = self._lib.lfgpu_create(device, ctypes.byref(h))
+        if rc != OK:
+            raise GpuError(rc, f"lfgpu_create failed with status {rc} (is a CUDA device visible?)")
+        self._h = h
+        self.n_dofs = 0
+        self.nnz = 0
+        self.n_elements = 0
+
+    # -- plumbing
+    def _check(self, rc: int) -> None:
+        if rc != OK:
+            msg = self._lib.lfgpu_last_error(self._h).decode()
+            raise GpuError(rc, msg)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.lfgpu_destroy(self._h)
+            self._h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- model
+    def set_mesh(self, xy, element_nodes, element_material, young, poisson, thickness, plane_mode: int) -> None:
+        xy = _arr(xy, np.float64).reshape(-1, 2)
+        en = _arr(element_nodes, np.int32).reshape(-1, 4)
+        em = _arr(element_material, np.int32).reshape(-1)
+        young = _arr(young, np.float64)
+        poisson = _arr(poisson, np.float64)
+        thickness = _arr(thickness, np.float64)
+        self._keep_mesh = (xy, en, em, young, poisson, thickness)
+        self._check(self._lib.lfgpu_set_mesh(self._h, xy.shape[0], _ptr(xy), en.shape[0], _ptr(en), _ptr(em),
+                                             young.shape[0], _ptr(young), _ptr(poisson), _ptr(thickness),
+                                             int(plane_mode)))
+        self.n_dofs = 2 * xy.shape[0]
+        self.n_elements = en.shape[0]
+
+    def set_young(self, young) -> None:
+        young = _arr(young, np.float64)
+        self._check(self._lib.lfgpu_set_young(self._h, _ptr(young)))
+
+    def set_pattern(self, row_offsets, columns, element_value_index, element_color=None) -> None:
+        rp = _arr(row_offsets, np.int64)
+        col = _arr(columns, np.int32)
+        mp = _arr(element_value_index, np.int32).reshape(-1)
+        colors = None if element_color is None else _arr(element_color, np.int32)
+        self._check(self._lib.lfgpu_set_pattern(self._h, rp.shape[0] - 1, col.shape[0], _ptr(rp), _ptr(col),
+                                                _ptr(mp), _ptr(colors)))
+        self.nnz = col.shape[0]
+
+    def build_pattern(self) -> None:
+        self._check(self._lib.lfgpu_build_pattern(self._h))
+        n, nnz, nc = c_int64(), c_int64(), c_int64()
+        self._check(self._lib.lfgpu_pattern_info(self._h, ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(nc)))
+        self.nnz = nnz.value
+        self.n_colors = nc.value
+
+    def download_pattern(self):
+        rp = np.empty(self.n_dofs + 1, np.int64)
+        col = np.empty(self.nnz, np.int32)
+        mp = np.empty(self.n_elements * 64, np.int32)
+        colors = np.empty(self.n_elements, np.int32)
+        self._check(self._lib.lfgpu_download_pattern(self._h, _ptr(rp), _ptr(col), _ptr(mp), _ptr(colors)))
+        return rp, col, mp.reshape(-1, 64), colors
+
+    def set_loads(self, nodal=None, body_element=None, body_bx=None, body_by=None, edge_element=None,
+                  edge_side=None, edge_kind=None, edge_first=None, edge_second=None) -> None:
+        nodal = None if nodal is None else _arr(nodal, np.float64)
+        nb = 0 if body_element is None else len(body_element)
+        ne = 0 if edge_element is None else len(edge_element)
+        be = _arr(body_element if nb else np.zeros(0), np.int32)
+        bx = _arr(body_bx if nb else np.zeros(0), np.float64)
+        by = _arr(body_by if nb else np.zeros(0), np.float64)
+        ee = _arr(edge_element if ne else np.zeros(0), np.int32)
+        es = _arr(edge_side if ne else np.zeros(0), np.int32)
+        ek = _arr(edge_kind if ne else np.zeros(0), np.int32)
+        ea = _arr(edge_first if ne else np.zeros(0), np.float64)
+        eb = _arr(edge_second if ne else np.zeros(0), np.float64)
+        self._check(self._lib.lfgpu_set_loads(self._h, _ptr(nodal), nb, _ptr(be), _ptr(bx), _ptr(by), ne,
+                                              _ptr(ee), _ptr(es), _ptr(ek), _ptr(ea), _ptr(eb)))
+
+    def set_constraints(self, dofs, values) -> None:
+        d = _arr(dofs, np.int64)
+        v = _arr(values, np.float64)
+        self._check(self._lib.lfgpu_set_constraints(self._h, d.shape[0], _ptr(d), _ptr(v)))
+
+    # -- solve path
+    def assemble(self, strategy: str = "coloring") -> None:
+        self._check(self._lib.lfgpu_assemble(self._h, ASSEMBLY[strategy]))
+
+    def apply_dirichlet(self) -> None:
+        self._check(self._lib.lfgpu_apply_dirichlet(self._h))
+
+    @staticmethod
+    def options(tolerance: float, max_iterations: int, storage: str = "csr", preconditioner: str = "jacobi",
+                precision: str = "fp64", refinement: str = "reliable", inner_reduction: float = 0.0,
+                max_refinements: int = 0) -> SolveOptions:
+        return SolveOptions(float(tolerance), int(max_iterations), STORAGE[storage], PRECOND[preconditioner],
+                            PRECISION[precision], REFINEMENT[refinement], float(inner_reduction),
+                            int(max_refinements))
+
+    def solve(self, options: SolveOptions, download: bool = True):
+        rep = Report()
+        u = np.empty(self.n_dofs) if download else None
+        rc = self._lib.lfgpu_solve(self._h, ctypes.byref(options), _ptr(u), ctypes.byref(rep))
+        if rc != OK:
+            msg = self._lib.lfgpu_last_error(self._h).decode()
+            err = GpuError(rc, msg)
+            err.report = rep
+            raise err
+        return u, rep
+
+    def reactions(self, download: bool = True):
+        r = np.empty(self.n_dofs) if download else None
+        self._check(self._lib.lfgpu_reactions(self._h, _ptr(r)))
+        return r
+
+    def download(self, which: int) -> np.ndarray:
+        size = self.nnz if which in (K_FULL, K_CONSTRAINED) else self.n_dofs
+        out = np.empty(size)
+        self._check(self._lib.lfgpu_download(self._h, which, _ptr(out)))
+        return out
+
+    def timings(self) -> dict:
+        t = Timings()
+        self._check(self._lib.lfgpu_timings_get(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def spmv(self, x, which: int = 1, storage: str = "csr", precision: str = "fp64", repeat: int = 1):
+        x = _arr(x, np.float64)
+        y = np.empty(self.n_dofs)
+        ms = c_double()
+        self._check(self._lib.lfgpu_spmv(self._h, which, STORAGE[storage], PRECISION[precision], _ptr(x), _ptr(y),
+                                         int(repeat), ctypes.byref(ms)))
+        return y, ms.value
+
+    def adjoint(self, dj_du=None, options: SolveOptions | None = None):
+        grad = np.empty(self.n_elements)
+        rep = Report()
+        d = None if dj_du is None else _arr(dj_du, np.float64)
+        self._check(self._lib.lfgpu_adjoint(self._h, _ptr(d), None if options is None else ctypes.byref(options),
+                                            _ptr(grad), ctypes.byref(rep)))
+        return grad, rep

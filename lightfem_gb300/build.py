@@ -1,0 +1,84 @@
+"""Build liblfgpu.so in-tree: every CUDA translation unit for sm_103a, compiled in
+parallel with nvcc, plus the host setup code with g++/OpenMP.
+
+    python -m lightfem_gb300.build          # or lightfem_gb300.build.build()
+
+Output: lightfem_gb300/_lib/liblfgpu.so (git-ignored; rebuilt on every machine).
+"""
+
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_lib")
+LIB = os.path.join(OUT_DIR, "liblfgpu.so")
+
+CUDA_SOURCES = ["api.cu", "assemble.cu", "sparse.cu", "pcg.cu", "ic0.cu", "adjoint.cu"]
+HOST_SOURCES = ["host_setup.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblfgpu")
+
+
+def _sources_newer(target: str) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "lfgpu.h"),
+                                                                  os.path.abspath(__file__)]
+    return any(os.path.getmtime(f) > t for f in files if os.path.isfile(f))
+
+
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
+    """Compile liblfgpu.so if any source is newer than it; return its path."""
+    if not force and not ptxas_info and not _sources_newer(LIB):
+        return LIB
+    os.makedirs(os.path.join(OUT_DIR, "obj"), exist_ok=True)
+    nv = nvcc()
+    inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
+    jobs = []
+    for src in CUDA_SOURCES:
+        obj = os.path.join(OUT_DIR, "obj", src + ".o")
+        cmd = [nv, *ARCH, "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler",
+               "-fPIC", *inc, "-c", os.path.join(CSRC, src), "-o", obj]
+        if ptxas_info:
+            cmd.insert(1, "-Xptxas=-v")
+        jobs.append((cmd, obj))
+    cxx = os.environ.get("CXX", "g++")
+    for src in HOST_SOURCES:
+        obj = os.path.join(OUT_DIR, "obj", src + ".o")
+        jobs.append(([cxx, "-O3", "-std=c++17", "-fPIC", "-fopenmp", *inc, "-c", os.path.join(CSRC, src),
+                      "-o", obj], obj))
+    procs = [(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True), cmd)
+             for cmd, _ in jobs]
+    failed = []
+    for p, cmd in procs:
+        out, _ = p.communicate()
+        if verbose or ptxas_info or p.returncode != 0:
+            sys.stderr.write(out)
+        if p.returncode != 0:
+            failed.append(" ".join(cmd))
+    if failed:
+        raise RuntimeError("liblfgpu build failed:\n" + "\n".join(failed))
+    tmp = LIB + ".tmp"
+    link = [nv, *ARCH, "-shared", "-o", tmp, *[obj for _, obj in jobs], "-Xcompiler", "-fopenmp", "-lgomp"]
+    r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("liblfgpu link failed:\n" + r.stdout)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True, ptxas_info="--ptxas" in sys.argv))

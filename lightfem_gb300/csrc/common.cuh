@@ -1,0 +1,303 @@
+// Shared internals of liblfgpu: the handle, device buffers, error plumbing and
+// the device-side building blocks (warp reductions, cache-hinted loads, the
+// bounded grid barrier) that every kernel file uses.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "lfgpu.h"
+
+namespace lfgpu {
+
+using i64 = long long;
+
+// ------------------------------------------------------------------ host errors
+struct Error {
+    int code;
+    std::string message;
+};
+
+#define LF_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t err_ = (call);                                                             \
+        if (err_ != cudaSuccess)                                                               \
+            throw ::lfgpu::Error{err_ == cudaErrorMemoryAllocation ? LFGPU_ERR_NOMEM : LFGPU_ERR_CUDA, \
+                                 std::string(#call) + ": " + cudaGetErrorString(err_)};        \
+    } while (0)
+
+#define LF_REQUIRE(cond, code, msg)                     \
+    do {                                                \
+        if (!(cond)) throw ::lfgpu::Error{(code), (msg)}; \
+    } while (0)
+
+// Device buffer that grows on demand and is released with the handle.
+template <typename T>
+struct Buf {
+    T* p = nullptr;
+    size_t count = 0;
+    void ensure(size_t n) {
+        if (n <= count && p != nullptr) return;
+        release();
+        if (n == 0) return;
+        // Round up to 64 elements so vectorised tails never leave the allocation.
+        const size_t padded = (n + 63) / 64 * 64;
+        LF_CUDA(cudaMalloc(reinterpret_cast<void**>(&p), padded * sizeof(T)));
+        count = n;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        count = 0;
+    }
+    operator T*() const { return p; }
+};
+
+// Device-side status word of one handle.  Kernels record the first failure here;
+// the host reads it after the stream synchronises.
+struct DeviceStatus {
+    int code;            // lfgpu_status of the first failure, 0 if none
+    int bad_index;       // element, row or block that caused it (smallest wins)
+    unsigned int abort;  // set when any CTA gives up a wait; every wait checks it
+    int pad;
+};
+
+// Result record the persistent PCG kernels write (CTA 0) at exit.
+struct PcgResult {
+    long long iterations;
+    long long refinements;
+    double initial_residual;
+    double final_residual;
+    int status;
+    int converged;
+    int stagnated;
+    int pad;
+};
+
+// Scalars of the grid-wide reductions: one slot per barrier of an iteration,
+// each slot holding up to kMaxReduce values per CTA.
+constexpr int kMaxReduce = 4;
+constexpr int kSlots = 4;
+
+struct Context {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    std::string error;
+
+    // mesh
+    i64 n_nodes = 0, n_elem = 0, n_mat = 0;
+    int plane_mode = 0;
+    Buf<double2> xy;
+    Buf<int4> elem_nodes;
+    Buf<int> elem_mat;
+    Buf<double> mat_young, mat_nu, mat_t;
+    std::vector<int> h_elem_nodes;  // host copy for setup work
+
+    // pattern
+    i64 n = 0, nnz = 0;
+    bool have_pattern = false;
+    bool paired = false;  // every row has even length and starts at an even offset with (2j, 2j+1) column pairs
+    Buf<int> rowptr, col, map, diag;
+    std::vector<int> h_rowptr_cache;
+    std::vector<int> h_colors;
+    int n_colors = 0;
+    std::vector<int> color_offsets;  // host, n_colors + 1
+    Buf<int> color_elems;
+
+    // loads
+    bool have_nodal = false;
+    Buf<double> f_nodal;
+    Buf<double> body_bx, body_by;  // per element, or empty
+    bool have_body = false;
+    Buf<int> edge_ptr;             // per element CSR over edge records (E + 1)
+    Buf<int> edge_side, edge_kind;
+    Buf<double> edge_a, edge_b;
+    bool have_edges = false;
+
+    // constraints
+    i64 n_constraints = 0;
+    Buf<unsigned char> fixed;
+    Buf<double> prescribed;
+
+    // system
+    Buf<double> K, K_full, f, f_full;
+    bool assembled = false, constrained = false;
+    unsigned long long k_version = 0;  // bumps when K changes: invalidates derived matrices
+
+    // derived matrices (built on first use per K version)
+    Buf<int> brow, bcol;
+    Buf<double> bval64;
+    Buf<float> bval32;
+    Buf<float> K32;
+    i64 nblocks = 0;
+    unsigned long long bsr_version = ~0ull, k32_version = ~0ull, b32_version = ~0ull;
+    double last_convert_ms = 0.0;
+
+    // preconditioners
+    Buf<double> inv_diag64, blk64;
+    Buf<float> inv_diag32, blk32;
+    unsigned long long pre_version = ~0ull;
+    i64 degenerate_blocks = 0;
+
+    // solve vectors and scratch
+    Buf<double> u, R;
+    Buf<double> v64[6];
+    Buf<float> v32[6];
+    Buf<double> partials;                 // kSlots * kMaxReduce * max CTAs
+    Buf<unsigned long long> bar;          // grid barrier counter
+    Buf<DeviceStatus> status;
+    Buf<PcgResult> pcg_result;
+    Buf<double> scratch64;
+    bool solved = false;
+
+    // ic0 state (built per K version)
+    unsigned long long ic0_version = ~0ull;
+    Buf<int> l_ptr, l_col, lt_ptr, lt_col, lt_src, fwd_rows, bwd_rows;
+    Buf<double> l_val, l_inv, lt_val;
+    Buf<float> l_val32, l_inv32, lt_val32;
+    std::vector<int> fwd_level_ptr, bwd_level_ptr;
+    i64 ic0_breakdowns = 0;
+
+    lfgpu_timings timings{};
+};
+
+void check_status(Context& c);   // syncs the stream, raises the first device failure
+void reset_status(Context& c);
+float elapsed_ms(Context& c);    // between ev_a and ev_b (synchronises ev_b)
+
+// ------------------------------------------------------------------ device side
+__device__ __forceinline__ void record_failure(DeviceStatus* s, int code, int index) {
+    if (atomicCAS(&s->code, 0, code) == 0 || s->code == code) atomicMin(&s->bad_index, index);
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Streaming loads for matrix data that is read once per product: evict-first in
+// L2 so the iteration vectors stay resident.
+__device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
+__device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
+__device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
+__device__ __forceinline__ double2 ld_stream(const double2* p) { return __ldcs(p); }
+__device__ __forceinline__ float4 ld_stream(const float4* p) { return __ldcs(p); }
+__device__ __forceinline__ int2 ld_stream(const int2* p) { return __ldcs(p); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// A wait that gives up after this long sets DeviceStatus::abort and returns.
+constexpr unsigned long long kWaitLimitNs = 4000000000ull;  // 4 s
+
+// Grid-wide barrier for cooperative launches, bounded in time.  Every CTA arrives
+// with a release add on a monotonically increasing counter and waits (acquire)
+// until all CTAs of this episode arrived.  Returns false if the wait ran out or
+// another CTA aborted; the caller then leaves its loop.
+__device__ __forceinline__ bool grid_barrier(unsigned long long* counter, unsigned long long target,
+                                             DeviceStatus* status, int* s_flag) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(counter), "l"(1ull) : "memory");
+        const unsigned long long start = global_ns();
+        int ok = 1;
+        while (true) {
+            unsigned long long seen;
+            asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(seen) : "l"(counter) : "memory");
+            if (seen >= target) break;
+            unsigned int ab;
+            asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(ab) : "l"(&status->abort) : "memory");
+            if (ab != 0u) {
+                ok = 0;
+                break;
+            }
+            if (global_ns() - start > kWaitLimitNs) {
+                atomicExch(&status->abort, 1u);
+                record_failure(status, LFGPU_ERR_TIMEOUT, static_cast<int>(blockIdx.x));
+                ok = 0;
+                break;
+            }
+        }
+        *s_flag = ok;
+    }
+    __syncthreads();
+    return *s_flag != 0;
+}
+
+// Sum K per-thread values over the CTA; thread 0 gets the totals.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double* s_red /* [32 * K] */) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) s_red[warp * K + k] = v[k];
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double t = lane < nw ? s_red[lane * K + k] : 0.0;
+            v[k] = warp_sum(t);
+        }
+    }
+    __syncthreads();
+}
+
+// Grid-wide sum of K values with a fixed reduction order (deterministic): each CTA
+// publishes its block sum in its slot, passes the barrier, then every CTA adds the
+// published values in CTA order.  Returns false when the barrier gave up.
+template <int K>
+__device__ __forceinline__ bool grid_sum(double (&v)[K], double* partials, int slot, unsigned long long* counter,
+                                         unsigned long long target, DeviceStatus* status, double* s_red,
+                                         int* s_flag) {
+    block_sum<K>(v, s_red);
+    double* mine = partials + (static_cast<size_t>(slot) * gridDim.x + blockIdx.x) * kMaxReduce;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) mine[k] = v[k];
+    }
+    if (!grid_barrier(counter, target, status, s_flag)) return false;
+    if (threadIdx.x < 32) {
+        const double* all = partials + static_cast<size_t>(slot) * gridDim.x * kMaxReduce;
+        double acc[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] = 0.0;
+        for (int b = threadIdx.x; b < static_cast<int>(gridDim.x); b += 32) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) acc[k] += all[static_cast<size_t>(b) * kMaxReduce + k];
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] = warp_sum(acc[k]);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) s_red[k] = acc[k];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = s_red[k];
+    __syncthreads();
+    return true;
+}
+
+inline int grid_for(i64 work, int block, int cap = 1 << 20) {
+    i64 g = (work + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return static_cast<int>(g);
+}
+
+}  // namespace lfgpu

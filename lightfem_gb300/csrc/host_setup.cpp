@@ -1,0 +1,195 @@
+// Host-side setup of the solve path: CSR pattern + element->value map, greedy
+// element colouring and reverse Cuthill-McKee ordering.  These produce exactly
+// what the reference produces (the pattern and map bit-for-bit), from flat arrays
+// and without hash containers.
+//
+//   build_pattern   build_csr_assembly_pattern + CsrMatrix::value_index,
+//                   src/sparse.cpp:15-74
+//   greedy_colors   element_colors, src/solver.cpp:100-133
+//   rcm_order       reverse_cuthill_mckee, src/reordering.cpp:11-62
+//
+// A Q4 element couples both DOFs of each of its nodes, so rows 2i and 2i+1 share
+// one column list {2j, 2j+1 : j in S(i)} where S(i) is the set of nodes sharing an
+// element with node i (i included).  The pattern is therefore built per node: the
+// sorted set S(i), then the two rows.  A node in no element keeps only its two
+// diagonal entries, as the reference's pattern does.
+#include "host_setup.hpp"
+
+#include <algorithm>
+#include <numeric>
+#include <queue>
+#include <stdexcept>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace lfgpu {
+
+namespace {
+
+// node -> elements touching it, in element order
+void node_elements(long long n_nodes, long long n_elem, const int* en, std::vector<long long>& ptr,
+                   std::vector<int>& list) {
+    ptr.assign(static_cast<size_t>(n_nodes) + 1, 0);
+    for (long long e = 0; e < n_elem; ++e)
+        for (int a = 0; a < 4; ++a) ++ptr[static_cast<size_t>(en[4 * e + a]) + 1];
+    for (long long i = 0; i < n_nodes; ++i) ptr[i + 1] += ptr[i];
+    list.resize(static_cast<size_t>(ptr[n_nodes]));
+    std::vector<long long> fill(ptr.begin(), ptr.end() - 1);
+    for (long long e = 0; e < n_elem; ++e)
+        for (int a = 0; a < 4; ++a) list[static_cast<size_t>(fill[en[4 * e + a]]++)] = static_cast<int>(e);
+}
+
+}  // namespace
+
+HostPattern build_pattern(long long n_nodes, long long n_elem, const int* en) {
+    HostPattern p;
+    std::vector<long long> nptr;
+    std::vector<int> nlist;
+    node_elements(n_nodes, n_elem, en, nptr, nlist);
+
+    // S(i) for every node.
+    std::vector<long long> sptr(static_cast<size_t>(n_nodes) + 1, 0);
+    std::vector<std::vector<int>> sets(static_cast<size_t>(n_nodes));
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long long i = 0; i < n_nodes; ++i) {
+        std::vector<int>& s = sets[static_cast<size_t>(i)];
+        for (long long k = nptr[i]; k < nptr[i + 1]; ++k) {
+            const int e = nlist[static_cast<size_t>(k)];
+            for (int a = 0; a < 4; ++a) s.push_back(en[4 * static_cast<long long>(e) + a]);
+        }
+        std::sort(s.begin(), s.end());
+        s.erase(std::unique(s.begin(), s.end()), s.end());
+    }
+    const long long n = 2 * n_nodes;
+    p.n = n;
+    p.rowptr.assign(static_cast<size_t>(n) + 1, 0);
+    for (long long i = 0; i < n_nodes; ++i) {
+        const long long len = sets[i].empty() ? 1 : 2 * static_cast<long long>(sets[i].size());
+        p.rowptr[2 * i + 1] = p.rowptr[2 * i] + len;
+        p.rowptr[2 * i + 2] = p.rowptr[2 * i + 1] + len;
+    }
+    p.nnz = p.rowptr[n];
+    if (p.nnz >= (1LL << 31)) throw std::length_error("pattern exceeds 2^31 nonzeros");
+    p.col.resize(static_cast<size_t>(p.nnz));
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < n_nodes; ++i) {
+        const std::vector<int>& s = sets[static_cast<size_t>(i)];
+        for (int half = 0; half < 2; ++half) {
+            int* out = p.col.data() + p.rowptr[2 * i + half];
+            if (s.empty()) {
+                out[0] = static_cast<int>(2 * i + half);
+                continue;
+            }
+            for (size_t k = 0; k < s.size(); ++k) {
+                out[2 * k] = 2 * s[k];
+                out[2 * k + 1] = 2 * s[k] + 1;
+            }
+        }
+    }
+    p.map.resize(static_cast<size_t>(n_elem) * 64);
+#pragma omp parallel for schedule(static)
+    for (long long e = 0; e < n_elem; ++e) {
+        const int* nd = en + 4 * e;
+        for (int a = 0; a < 4; ++a) {
+            const std::vector<int>& s = sets[static_cast<size_t>(nd[a])];
+            for (int b = 0; b < 4; ++b) {
+                const int pos = static_cast<int>(std::lower_bound(s.begin(), s.end(), nd[b]) - s.begin());
+                for (int i = 0; i < 2; ++i) {
+                    const long long row = 2LL * nd[a] + i;
+                    const long long base = p.rowptr[row] + 2LL * pos;
+                    p.map[static_cast<size_t>(e) * 64 + (2 * a + i) * 8 + 2 * b] = static_cast<int>(base);
+                    p.map[static_cast<size_t>(e) * 64 + (2 * a + i) * 8 + 2 * b + 1] = static_cast<int>(base + 1);
+                }
+            }
+        }
+    }
+    return p;
+}
+
+int greedy_colors(long long n_nodes, long long n_elem, const int* en, std::vector<int>& colors) {
+    std::vector<long long> nptr;
+    std::vector<int> nlist;
+    node_elements(n_nodes, n_elem, en, nptr, nlist);
+    colors.assign(static_cast<size_t>(n_elem), -1);
+    std::vector<long long> stamp(static_cast<size_t>(n_elem) + 1, -1);
+    int top = -1;
+    for (long long e = 0; e < n_elem; ++e) {
+        for (int a = 0; a < 4; ++a) {
+            const int nd = en[4 * e + a];
+            for (long long k = nptr[nd]; k < nptr[nd + 1]; ++k) {
+                const int o = colors[static_cast<size_t>(nlist[static_cast<size_t>(k)])];
+                if (o >= 0) stamp[static_cast<size_t>(o)] = e;
+            }
+        }
+        int c = 0;
+        while (stamp[static_cast<size_t>(c)] == e) ++c;
+        colors[static_cast<size_t>(e)] = c;
+        top = std::max(top, c);
+    }
+    return top + 1;
+}
+
+void rcm_order(long long n_nodes, const long long* ids, long long n_elem, const long long* elem_ids,
+               long long* order) {
+    // Work on node indices in ascending-ID order; ties in degree break by ID,
+    // which is the index order here.
+    std::vector<long long> sorted(ids, ids + n_nodes);
+    std::sort(sorted.begin(), sorted.end());
+    auto index_of = [&](long long id) {
+        const auto it = std::lower_bound(sorted.begin(), sorted.end(), id);
+        if (it == sorted.end() || *it != id) throw std::invalid_argument("element references an unknown node ID");
+        return static_cast<int>(it - sorted.begin());
+    };
+    std::vector<int> en(static_cast<size_t>(n_elem) * 4);
+    for (long long k = 0; k < 4 * n_elem; ++k) en[static_cast<size_t>(k)] = index_of(elem_ids[k]);
+    std::vector<long long> nptr;
+    std::vector<int> nlist;
+    node_elements(n_nodes, n_elem, en.data(), nptr, nlist);
+    std::vector<std::vector<int>> adj(static_cast<size_t>(n_nodes));
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long long i = 0; i < n_nodes; ++i) {
+        std::vector<int>& s = adj[static_cast<size_t>(i)];
+        for (long long k = nptr[i]; k < nptr[i + 1]; ++k) {
+            const int e = nlist[static_cast<size_t>(k)];
+            for (int a = 0; a < 4; ++a) {
+                const int j = en[4 * static_cast<size_t>(e) + a];
+                if (j != i) s.push_back(j);
+            }
+        }
+        std::sort(s.begin(), s.end());
+        s.erase(std::unique(s.begin(), s.end()), s.end());
+    }
+    auto before = [&](int a, int b) {
+        const size_t da = adj[static_cast<size_t>(a)].size(), db = adj[static_cast<size_t>(b)].size();
+        return da != db ? da < db : a < b;
+    };
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (long long i = 0; i < n_nodes; ++i) std::sort(adj[i].begin(), adj[i].end(), before);
+    std::vector<int> seeds(static_cast<size_t>(n_nodes));
+    std::iota(seeds.begin(), seeds.end(), 0);
+    std::stable_sort(seeds.begin(), seeds.end(), before);
+    std::vector<char> seen(static_cast<size_t>(n_nodes), 0);
+    std::vector<int> out;
+    out.reserve(static_cast<size_t>(n_nodes));
+    std::vector<int> fifo(static_cast<size_t>(n_nodes));
+    for (const int s : seeds) {
+        if (seen[static_cast<size_t>(s)]) continue;
+        seen[static_cast<size_t>(s)] = 1;
+        size_t head = 0, tail = 0;
+        fifo[tail++] = s;
+        while (head < tail) {
+            const int cur = fifo[head++];
+            out.push_back(cur);
+            for (const int v : adj[static_cast<size_t>(cur)])
+                if (!seen[static_cast<size_t>(v)]) {
+                    seen[static_cast<size_t>(v)] = 1;
+                    fifo[tail++] = v;
+                }
+        }
+    }
+    for (long long k = 0; k < n_nodes; ++k) order[k] = sorted[static_cast<size_t>(out[static_cast<size_t>(n_nodes - 1 - k)])];
+}
+
+}  // namespace lfgpu

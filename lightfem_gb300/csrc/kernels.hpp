@@ -1,0 +1,49 @@
+// Launchers each kernel file exports to the C ABI layer (api.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace lfgpu {
+
+// assemble.cu
+void launch_assembly(Context& c, int strategy);
+
+// sparse.cu
+void launch_find_diagonal(Context& c);
+void launch_dirichlet(Context& c);           // elimination + zero-pivot sweep, in place on K, f
+void launch_spmv_csr64(Context& c, const double* val, const double* x, double* y, const double* sub);
+void launch_spmv_csr32(Context& c, const float* val, const float* x, float* y);
+void launch_spmv_bsr64(Context& c, const double* x, double* y);
+void launch_spmv_bsr32(Context& c, const float* x, float* y);
+void ensure_bsr(Context& c);                 // BSR structure + FP64 values of K (constrained)
+void ensure_bsr32(Context& c);
+void ensure_csr32(Context& c);
+void ensure_preconditioners(Context& c);     // Jacobi inverse diagonal and 2x2 nodal factors
+void launch_to_float(Context& c, const double* in, float* out, i64 count);
+double device_norm2(Context& c, const double* v, i64 count);      // synchronous helper
+void launch_axpby(Context& c, i64 count, double a, const double* x, double b, double* y);
+
+// pcg.cu
+struct SolveSetup {
+    int storage;
+    int precond;
+    double tolerance;
+    i64 max_iterations;
+    int mixed;
+    int restart;
+    double inner_reduction;
+    i64 max_refinements;
+    const double* x0;  // FP64 warm start or nullptr (x0 = 0)
+    const double* rhs; // right-hand side (device)
+    double* x;         // FP64 solution (device)
+};
+PcgResult run_pcg(Context& c, const SolveSetup& s, float* kernel_ms);
+
+// ic0.cu
+void ensure_ic0(Context& c, bool fp32);
+PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double* apply_ms);
+
+// adjoint.cu
+void launch_adjoint_grad(Context& c, const double* u, const double* lam, double* grad);
+
+}  // namespace lfgpu

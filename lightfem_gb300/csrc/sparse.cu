@@ -1,0 +1,475 @@
+// Sparse-matrix kernels of the solve path: diagonal lookup, symmetric Dirichlet
+// elimination, CSR and 2x2-BSR products in FP64 and FP32, CSR->BSR conversion,
+// FP32 copies and the Jacobi / 2x2 nodal block-Jacobi setup.
+//
+// All of these are bandwidth-bound.  Products use a quarter warp per row (CSR) or
+// per block row (BSR) so a warp reads eight rows' contiguous value/column streams
+// at once; matrix data is loaded with the streaming (evict-first) hint so the
+// dense vectors stay resident in the 129 MB L2.
+#include "common.cuh"
+#include "kernels.hpp"
+
+#include <cmath>
+
+namespace lfgpu {
+namespace {
+
+constexpr int kThreads = 256;
+
+__global__ void find_diagonal_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                     int* __restrict__ diag) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    int lo = rowptr[r], hi = rowptr[r + 1];
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (col[mid] < r) lo = mid + 1;
+        else hi = mid;
+    }
+    diag[r] = (lo < rowptr[r + 1] && col[lo] == r) ? lo : -1;
+}
+
+// apply_dirichlet, src/solver.cpp:386-412.  One thread per row, entries in column
+// order, products and differences rounded separately exactly as the host code
+// rounds them, so K and f come out bit-identical to the reference.
+__global__ void dirichlet_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                 const int* __restrict__ diag, const unsigned char* __restrict__ fixed,
+                                 const double* __restrict__ prescribed, double* __restrict__ K, double* __restrict__ f) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int b = rowptr[r], e = rowptr[r + 1];
+    if (fixed[r]) {
+        for (int k = b; k < e; ++k) K[k] = 0.0;
+        K[diag[r]] = 1.0;
+        f[r] = prescribed[r];
+        return;
+    }
+    double fr = f[r];
+    bool touched = false;
+    for (int k = b; k < e; ++k) {
+        const int c = col[k];
+        if (!fixed[c]) continue;
+        const double v = K[k];
+        if (v == 0.0) continue;
+        fr = __dsub_rn(fr, __dmul_rn(v, prescribed[c]));
+        K[k] = 0.0;
+        touched = true;
+    }
+    if (touched) f[r] = fr;
+}
+
+__global__ void abs_max_kernel(int n, const double* __restrict__ v, unsigned long long* __restrict__ out) {
+    double m = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = fmax(m, fabs(v[i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, static_cast<unsigned long long>(__double_as_longlong(m)));
+}
+
+// Zero-pivot sweep, src/solver.cpp:920-940.
+__global__ void zero_pivot_kernel(int n, const int* __restrict__ diag, const unsigned long long* __restrict__ scale_bits,
+                                  double* __restrict__ K, double* __restrict__ f, DeviceStatus* status) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double scale = __longlong_as_double(static_cast<long long>(*scale_bits));
+    if (scale <= 0.0) scale = 1.0;
+    const double d = K[diag[r]];
+    if (fabs(d) > 1.0e-30) return;
+    if (fabs(f[r]) > 1.0e-12 * scale) {
+        record_failure(status, LFGPU_ERR_MECHANISM, r);
+        return;
+    }
+    K[diag[r]] = 1.0;
+    f[r] = 0.0;
+}
+
+// ---------------------------------------------------------------- products
+template <typename T>
+__global__ void __launch_bounds__(kThreads) spmv_csr_kernel(int n, const int* __restrict__ rowptr,
+                                                            const int* __restrict__ col, const T* __restrict__ val,
+                                                            const T* __restrict__ x, T* __restrict__ y,
+                                                            const T* __restrict__ sub) {
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+    const int q = threadIdx.x & 3;
+    T s = T(0);
+    if (row < n) {
+        const int b = __ldg(rowptr + row), e = __ldg(rowptr + row + 1);
+        for (int k = b + q; k < e; k += 4) s += ld_stream(val + k) * x[ld_stream(col + k)];
+    }
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (row < n && q == 0) y[row] = sub ? s - sub[row] : s;
+}
+
+__global__ void __launch_bounds__(kThreads) spmv_bsr64_kernel(int nb, const int* __restrict__ brow,
+                                                              const int* __restrict__ bcol,
+                                                              const double2* __restrict__ bval,
+                                                              const double2* __restrict__ x, double2* __restrict__ y) {
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+    const int q = threadIdx.x & 3;
+    double s0 = 0.0, s1 = 0.0;
+    if (row < nb) {
+        const int b = __ldg(brow + row), e = __ldg(brow + row + 1);
+        for (int k = b + q; k < e; k += 4) {
+            const double2 top = ld_stream(bval + 2 * static_cast<size_t>(k));
+            const double2 bot = ld_stream(bval + 2 * static_cast<size_t>(k) + 1);
+            const double2 xv = x[ld_stream(bcol + k)];
+            s0 += top.x * xv.x + top.y * xv.y;
+            s1 += bot.x * xv.x + bot.y * xv.y;
+        }
+    }
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+    if (row < nb && q == 0) y[row] = make_double2(s0, s1);
+}
+
+__global__ void __launch_bounds__(kThreads) spmv_bsr32_kernel(int nb, const int* __restrict__ brow,
+                                                              const int* __restrict__ bcol,
+                                                              const float4* __restrict__ bval,
+                                                              const float2* __restrict__ x, float2* __restrict__ y) {
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+    const int q = threadIdx.x & 3;
+    float s0 = 0.f, s1 = 0.f;
+    if (row < nb) {
+        const int b = __ldg(brow + row), e = __ldg(brow + row + 1);
+        for (int k = b + q; k < e; k += 4) {
+            const float4 v = ld_stream(bval + k);
+            const float2 xv = x[ld_stream(bcol + k)];
+            s0 += v.x * xv.x + v.y * xv.y;
+            s1 += v.z * xv.x + v.w * xv.y;
+        }
+    }
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+    if (row < nb && q == 0) y[row] = make_float2(s0, s1);
+}
+
+// ---------------------------------------------------------------- CSR -> BSR
+// Paired patterns (rows 2i and 2i+1 share one column list made of (2j, 2j+1)
+// pairs): block row i starts at rowptr[2i] / 4 and block k of it is a pure gather.
+__global__ void bsr_paired_structure_kernel(int nb, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                            int* __restrict__ brow, int* __restrict__ bcol) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > nb) return;
+    if (i == nb) {
+        brow[nb] = rowptr[2 * nb] / 4;
+        return;
+    }
+    const int b = rowptr[2 * i], e = rowptr[2 * i + 1];
+    const int out = b / 4;
+    brow[i] = out;
+    for (int k = b; k < e; k += 2) bcol[out + (k - b) / 2] = col[k] >> 1;
+}
+
+__global__ void bsr_paired_values_kernel(int nb, const int* __restrict__ rowptr, const int* __restrict__ brow,
+                                         const double* __restrict__ K, double2* __restrict__ bval) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= nb) return;
+    const int b0 = rowptr[2 * i], b1 = rowptr[2 * i + 1];
+    const int len = (b1 - b0) / 2;
+    const int out = brow[i];
+    for (int m = 0; m < len; ++m) {
+        const double2 top = *reinterpret_cast<const double2*>(K + b0 + 2 * m);
+        const double2 bot = *reinterpret_cast<const double2*>(K + b1 + 2 * m);
+        bval[2 * static_cast<size_t>(out + m)] = top;
+        bval[2 * static_cast<size_t>(out + m) + 1] = bot;
+    }
+}
+
+// General patterns: merge walk of the two rows of each block row
+// (BsrMatrix::from_csr, src/sparse.cpp:128-177).  Pass 1 counts, pass 2 fills.
+__device__ __forceinline__ int merge_walk(int i, const int* rowptr, const int* col, const double* K, int* bcol,
+                                          double2* bval, bool fill, int out) {
+    int p0 = rowptr[2 * i], p1 = rowptr[2 * i + 1];
+    const int e0 = rowptr[2 * i + 1], e1 = rowptr[2 * i + 2];
+    int count = 0;
+    while (p0 < e0 || p1 < e1) {
+        const int c0 = p0 < e0 ? col[p0] : 0x7fffffff;
+        const int c1 = p1 < e1 ? col[p1] : 0x7fffffff;
+        const int bc = min(c0, c1) >> 1;
+        double blk[4] = {0.0, 0.0, 0.0, 0.0};
+        for (; p0 < e0 && (col[p0] >> 1) == bc; ++p0) blk[col[p0] - 2 * bc] = K[p0];
+        for (; p1 < e1 && (col[p1] >> 1) == bc; ++p1) blk[2 + col[p1] - 2 * bc] = K[p1];
+        if (fill) {
+            bcol[out + count] = bc;
+            bval[2 * static_cast<size_t>(out + count)] = make_double2(blk[0], blk[1]);
+            bval[2 * static_cast<size_t>(out + count) + 1] = make_double2(blk[2], blk[3]);
+        }
+        ++count;
+    }
+    return count;
+}
+
+__global__ void bsr_count_kernel(int nb, const int* rowptr, const int* col, int* counts) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nb) counts[i] = merge_walk(i, rowptr, col, nullptr, nullptr, nullptr, false, 0);
+}
+
+__global__ void bsr_fill_kernel(int nb, const int* rowptr, const int* col, const double* K, const int* brow,
+                                int* bcol, double2* bval) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nb) merge_walk(i, rowptr, col, K, bcol, bval, true, brow[i]);
+}
+
+__global__ void to_float_kernel(i64 count, const double* __restrict__ in, float* __restrict__ out) {
+    for (i64 i = blockIdx.x * static_cast<i64>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<i64>(gridDim.x) * blockDim.x)
+        out[i] = static_cast<float>(in[i]);
+}
+
+// ---------------------------------------------------------------- preconditioners
+// inverse_diagonal_of (src/solver.cpp:656-669) and the 2x2 nodal case of
+// SubdomainBlockJacobi (src/precond.cpp:186-231): Cholesky of
+// [[K(2i,2i), .], [K(2i+1,2i), K(2i+1,2i+1)]] with reciprocal pivots stored as
+// (1/L00, L10, 1/L11); a block that is not positive definite becomes the identity.
+__global__ void precond_setup_kernel(int nb, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                     const int* __restrict__ diag, const double* __restrict__ K,
+                                     double* __restrict__ inv_diag, double* __restrict__ blk,
+                                     int* __restrict__ degenerate, DeviceStatus* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    const double d0 = K[diag[2 * i]], d1 = K[diag[2 * i + 1]];
+    if (!isfinite(d0) || !isfinite(d1)) record_failure(status, LFGPU_ERR_NONFINITE_DIAG, 2 * i);
+    inv_diag[2 * i] = fabs(d0) > 1.0e-30 ? 1.0 / d0 : 1.0;
+    inv_diag[2 * i + 1] = fabs(d1) > 1.0e-30 ? 1.0 / d1 : 1.0;
+    // K(2i+1, 2i): search row 2i+1 for column 2i.
+    double d10 = 0.0;
+    for (int k = rowptr[2 * i + 1]; k < rowptr[2 * i + 2]; ++k) {
+        if (col[k] == 2 * i) {
+            d10 = K[k];
+            break;
+        }
+        if (col[k] > 2 * i) break;
+    }
+    double f0 = 1.0, f1 = 0.0, f2 = 1.0;
+    bool ok = d0 > 0.0 && isfinite(d0);
+    if (ok) {
+        const double l00 = sqrt(d0);
+        const double l10 = d10 / l00;
+        const double s = d1 - l10 * l10;
+        ok = s > 0.0 && isfinite(s);
+        if (ok) {
+            const double l11 = sqrt(s);
+            f0 = 1.0 / l00;
+            f1 = l10;
+            f2 = 1.0 / l11;
+        }
+    }
+    if (!ok) {
+        f0 = 1.0;
+        f1 = 0.0;
+        f2 = 1.0;
+        atomicAdd(degenerate, 1);
+    }
+    blk[3 * i] = f0;
+    blk[3 * i + 1] = f1;
+    blk[3 * i + 2] = f2;
+}
+
+__global__ void norm_partials_kernel(i64 n, const double* __restrict__ v, double* __restrict__ partial) {
+    double s = 0.0;
+    for (i64 i = blockIdx.x * static_cast<i64>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<i64>(gridDim.x) * blockDim.x)
+        s += v[i] * v[i];
+    __shared__ double red[32];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        s = warp_sum(s);
+        if (threadIdx.x == 0) partial[blockIdx.x] = s;
+    }
+}
+
+__global__ void sum_partials_kernel(int m, const double* __restrict__ partial, double* __restrict__ out) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < m; i += 32) s += partial[i];
+    s = warp_sum(s);
+    if (threadIdx.x == 0) out[0] = s;
+}
+
+__global__ void axpby_kernel(i64 n, double a, const double* __restrict__ x, double b, double* __restrict__ y) {
+    for (i64 i = blockIdx.x * static_cast<i64>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<i64>(gridDim.x) * blockDim.x)
+        y[i] = a * x[i] + b * y[i];
+}
+
+__global__ void capture_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                               unsigned long long* __restrict__ inside) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long cnt = 0;
+    if (r < n)
+        for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) cnt += (col[k] >> 1) == (r >> 1);
+    cnt = warp_sum(cnt);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(inside, cnt);
+}
+
+}  // namespace
+
+void launch_find_diagonal(Context& c) {
+    find_diagonal_kernel<<<grid_for(c.n, kThreads), kThreads, 0, c.stream>>>(static_cast<int>(c.n), c.rowptr, c.col,
+                                                                            c.diag);
+    LF_CUDA(cudaGetLastError());
+}
+
+void launch_dirichlet(Context& c) {
+    const int n = static_cast<int>(c.n);
+    if (c.n_constraints > 0) {
+        dirichlet_kernel<<<grid_for(n, kThreads), kThreads, 0, c.stream>>>(n, c.rowptr, c.col, c.diag, c.fixed,
+                                                                          c.prescribed, c.K, c.f);
+        LF_CUDA(cudaGetLastError());
+    }
+    c.scratch64.ensure(64);
+    unsigned long long* bits = reinterpret_cast<unsigned long long*>(c.scratch64.p);
+    LF_CUDA(cudaMemsetAsync(bits, 0, sizeof(unsigned long long), c.stream));
+    abs_max_kernel<<<grid_for(n, kThreads, 4 * c.num_sms), kThreads, 0, c.stream>>>(n, c.f, bits);
+    zero_pivot_kernel<<<grid_for(n, kThreads), kThreads, 0, c.stream>>>(n, c.diag, bits, c.K, c.f, c.status);
+    LF_CUDA(cudaGetLastError());
+}
+
+void launch_spmv_csr64(Context& c, const double* val, const double* x, double* y, const double* sub) {
+    const int n = static_cast<int>(c.n);
+    spmv_csr_kernel<double><<<grid_for(4LL * n, kThreads), kThreads, 0, c.stream>>>(n, c.rowptr, c.col, val, x, y,
+                                                                                   sub);
+    LF_CUDA(cudaGetLastError());
+}
+
+void launch_spmv_csr32(Context& c, const float* val, const float* x, float* y) {
+    const int n = static_cast<int>(c.n);
+    spmv_csr_kernel<float><<<grid_for(4LL * n, kThreads), kThreads, 0, c.stream>>>(n, c.rowptr, c.col, val, x, y,
+                                                                                  nullptr);
+    LF_CUDA(cudaGetLastError());
+}
+
+void launch_spmv_bsr64(Context& c, const double* x, double* y) {
+    const int nb = static_cast<int>(c.n / 2);
+    spmv_bsr64_kernel<<<grid_for(4LL * nb, kThreads), kThreads, 0, c.stream>>>(
+        nb, c.brow, c.bcol, reinterpret_cast<const double2*>(c.bval64.p), reinterpret_cast<const double2*>(x),
+        reinterpret_cast<double2*>(y));
+    LF_CUDA(cudaGetLastError());
+}
+
+void launch_spmv_bsr32(Context& c, const float* x, float* y) {
+    const int nb = static_cast<int>(c.n / 2);
+    spmv_bsr32_kernel<<<grid_for(4LL * nb, kThreads), kThreads, 0, c.stream>>>(
+        nb, c.brow, c.bcol, reinterpret_cast<const float4*>(c.bval32.p), reinterpret_cast<const float2*>(x),
+        reinterpret_cast<float2*>(y));
+    LF_CUDA(cudaGetLastError());
+}
+
+void ensure_bsr(Context& c) {
+    if (c.bsr_version == c.k_version) return;
+    LF_REQUIRE(c.n % 2 == 0, LFGPU_ERR_ARGUMENT, "BSR conversion needs an even number of rows (u,v DOF pairs)");
+    const int nb = static_cast<int>(c.n / 2);
+    LF_CUDA(cudaEventRecord(c.ev_a, c.stream));
+    c.brow.ensure(nb + 1);
+    if (c.paired) {
+        c.nblocks = c.nnz / 4;
+        c.bcol.ensure(c.nblocks);
+        c.bval64.ensure(4 * c.nblocks);
+        bsr_paired_structure_kernel<<<grid_for(nb + 1, kThreads), kThreads, 0, c.stream>>>(nb, c.rowptr, c.col,
+                                                                                          c.brow, c.bcol);
+        bsr_paired_values_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(
+            nb, c.rowptr, c.brow, c.K, reinterpret_cast<double2*>(c.bval64.p));
+    } else {
+        Buf<int> counts;
+        counts.ensure(nb);
+        bsr_count_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(nb, c.rowptr, c.col, counts);
+        std::vector<int> h(nb), ptr(nb + 1, 0);
+        LF_CUDA(cudaMemcpyAsync(h.data(), counts.p, sizeof(int) * nb, cudaMemcpyDeviceToHost, c.stream));
+        LF_CUDA(cudaStreamSynchronize(c.stream));
+        for (int i = 0; i < nb; ++i) ptr[i + 1] = ptr[i] + h[i];
+        c.nblocks = ptr[nb];
+        LF_CUDA(cudaMemcpyAsync(c.brow.p, ptr.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, c.stream));
+        c.bcol.ensure(c.nblocks);
+        c.bval64.ensure(4 * c.nblocks);
+        bsr_fill_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(
+            nb, c.rowptr, c.col, c.K, c.brow, c.bcol, reinterpret_cast<double2*>(c.bval64.p));
+        LF_CUDA(cudaStreamSynchronize(c.stream));
+        counts.release();
+    }
+    LF_CUDA(cudaGetLastError());
+    LF_CUDA(cudaEventRecord(c.ev_b, c.stream));
+    c.last_convert_ms = elapsed_ms(c);
+    c.bsr_version = c.k_version;
+}
+
+void launch_to_float(Context& c, const double* in, float* out, i64 count) {
+    to_float_kernel<<<grid_for(count, kThreads, 16 * c.num_sms), kThreads, 0, c.stream>>>(count, in, out);
+    LF_CUDA(cudaGetLastError());
+}
+
+void ensure_bsr32(Context& c) {
+    ensure_bsr(c);
+    if (c.b32_version == c.k_version) return;
+    c.bval32.ensure(4 * c.nblocks);
+    launch_to_float(c, c.bval64, c.bval32, 4 * c.nblocks);
+    c.b32_version = c.k_version;
+}
+
+void ensure_csr32(Context& c) {
+    if (c.k32_version == c.k_version) return;
+    c.K32.ensure(c.nnz);
+    launch_to_float(c, c.K, c.K32, c.nnz);
+    c.k32_version = c.k_version;
+}
+
+void ensure_preconditioners(Context& c) {
+    if (c.pre_version == c.k_version) return;
+    const int nb = static_cast<int>(c.n / 2);
+    c.inv_diag64.ensure(c.n);
+    c.blk64.ensure(3 * static_cast<size_t>(nb));
+    c.inv_diag32.ensure(c.n);
+    c.blk32.ensure(3 * static_cast<size_t>(nb));
+    c.scratch64.ensure(64);
+    int* degenerate = reinterpret_cast<int*>(c.scratch64.p + 8);
+    LF_CUDA(cudaMemsetAsync(degenerate, 0, sizeof(int), c.stream));
+    precond_setup_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(nb, c.rowptr, c.col, c.diag, c.K,
+                                                                           c.inv_diag64, c.blk64, degenerate,
+                                                                           c.status);
+    LF_CUDA(cudaGetLastError());
+    launch_to_float(c, c.inv_diag64, c.inv_diag32, c.n);
+    launch_to_float(c, c.blk64, c.blk32, 3LL * nb);
+    int h = 0;
+    LF_CUDA(cudaMemcpyAsync(&h, degenerate, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    check_status(c);
+    c.degenerate_blocks = h;
+    c.pre_version = c.k_version;
+}
+
+double device_norm2(Context& c, const double* v, i64 count) {
+    const int blocks = 2 * c.num_sms;
+    c.scratch64.ensure(64 + blocks + 1);
+    double* partial = c.scratch64.p + 64;
+    norm_partials_kernel<<<blocks, kThreads, 0, c.stream>>>(count, v, partial);
+    sum_partials_kernel<<<1, 32, 0, c.stream>>>(blocks, partial, partial + blocks);
+    LF_CUDA(cudaGetLastError());
+    double h = 0.0;
+    LF_CUDA(cudaMemcpyAsync(&h, partial + blocks, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    LF_CUDA(cudaStreamSynchronize(c.stream));
+    return std::sqrt(h);
+}
+
+void launch_axpby(Context& c, i64 count, double a, const double* x, double b, double* y) {
+    axpby_kernel<<<grid_for(count, kThreads, 16 * c.num_sms), kThreads, 0, c.stream>>>(count, a, x, b, y);
+    LF_CUDA(cudaGetLastError());
+}
+
+double capture_ratio_2x2(Context& c) {
+    c.scratch64.ensure(64);
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(c.scratch64.p + 16);
+    LF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c.stream));
+    capture_kernel<<<grid_for(c.n, kThreads), kThreads, 0, c.stream>>>(static_cast<int>(c.n), c.rowptr, c.col, cnt);
+    LF_CUDA(cudaGetLastError());
+    unsigned long long h = 0;
+    LF_CUDA(cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
+    LF_CUDA(cudaStreamSynchronize(c.stream));
+    return c.nnz ? static_cast<double>(h) / static_cast<double>(c.nnz) : 0.0;
+}
+
+}  // namespace lfgpu

@@ -1,0 +1,178 @@
+"""``LinearElasticSolver.solve(model) -> AnalysisResult`` on the GPU.
+
+Mirrors the reference's top-level solve (``LinearElasticSolver::solve``,
+src/solver.cpp:875-960) stage by stage, with every numeric stage running in
+liblfgpu through the C ABI:
+
+    reordering (RCM, src/solver.cpp:886-892)        host, lfgpu_host_rcm
+    pattern + map + colours (src/solver.cpp:228-235) host C++ inside liblfgpu
+    element stiffness + assembly + loads             lfgpu_assemble
+    retain K, f; Dirichlet; zero-pivot sweep         lfgpu_apply_dirichlet
+    solve_iterative (src/solver.cpp:675-747)         lfgpu_solve
+    reactions (src/solver.cpp:953-954)               lfgpu_reactions
+
+Errors keep the reference's wording and exception kinds: a failed solve raises
+``RuntimeError`` with the message ``pcg_solve`` throws, non-convergence raises
+``RuntimeError("PCG did not converge: ...")`` (src/solver.cpp:948-950).
+Post-processing and VTK/CSV output stay with the reference host library.
+"""
+
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native
+from .model import Model
+
+
+@dataclass
+class CsrMatrix:
+    row_offsets: np.ndarray
+    column_indices: np.ndarray
+    values: np.ndarray
+
+    def rows(self) -> int:
+        return self.row_offsets.shape[0] - 1
+
+    def nonzeros(self) -> int:
+        return self.values.shape[0]
+
+
+@dataclass
+class LinearSolverReport:
+    """``LinearSolverReport`` (include/lightfem/solver.hpp:12-34) plus GPU fields."""
+
+    converged: bool = False
+    iterations: int = 0
+    initial_residual: float = 0.0
+    final_residual: float = 0.0
+    message: str = ""
+    preconditioner: str = "jacobi"
+    solve_ms: float = 0.0
+    matvec_ms: float = 0.0
+    matvec_calls: int = 0
+    storage: str = "csr"
+    matrix_bytes_per_matvec: int = 0
+    storage_convert_ms: float = 0.0
+    preconditioner_setup_ms: float = 0.0
+    preconditioner_apply_ms: float = 0.0
+    subdomains: int = 0
+    capture_ratio: float = 0.0
+    precision: str = "fp64"
+    refinements: int = 0
+    true_residual: float = 0.0
+    fallback_fp64: bool = False
+    ic0_breakdowns: int = 0
+
+
+@dataclass
+class PerformanceReport:
+    reordering: str = "none"
+    assembly: str = "coloring"
+    coloring_count: int = 0
+    pattern_ms: float = 0.0
+    element_stiffness_ms: float = 0.0
+    assembly_ms: float = 0.0
+    boundary_ms: float = 0.0
+    retain_matrix_ms: float = 0.0
+    postprocess_ms: float = 0.0
+    total_ms: float = 0.0
+
+
+@dataclass
+class AnalysisResult:
+    stiffness: CsrMatrix | None
+    load: np.ndarray
+    displacement: np.ndarray
+    reaction: np.ndarray
+    solver: LinearSolverReport
+    performance: PerformanceReport = field(default_factory=PerformanceReport)
+
+
+_MESSAGES = {
+    _native.ERR_NOT_SPD: "PCG encountered non-positive curvature; system is not SPD",
+    _native.ERR_RHO_INITIAL: "PCG failed to form a positive initial preconditioned residual",
+    _native.ERR_RHO: "PCG preconditioned residual became non-positive or non-finite",
+}
+
+
+def solve_options(settings) -> _native.SolveOptions:
+    return _native.Context.options(settings.tolerance, settings.max_iterations, settings.storage,
+                                   settings.preconditioner, settings.precision, settings.refinement)
+
+
+def upload_model(ctx: _native.Context, model: Model) -> None:
+    """Mesh, pattern, loads and constraints of an indexed model into ``ctx``."""
+    en = model.element_node_index()
+    ctx.set_mesh(model.xy, en, model.material_index(model.element_material), model.young, model.poisson,
+                 model.thickness, model.settings.plane_mode)
+    ctx.build_pattern()
+    body_e = model.element_index(model.body_element) if model.body_element.size else None
+    edge_e = model.element_index(model.edge_element) if model.edge_element.size else None
+    ctx.set_loads(model.nodal_load_vector(), body_e, model.body_bx, model.body_by, edge_e, model.edge_side,
+                  model.edge_kind, model.edge_first, model.edge_second)
+    dofs, vals = model.constraints()
+    ctx.set_constraints(dofs, vals)
+
+
+class LinearElasticSolver:
+    """GPU drop-in for ``lightfem::LinearElasticSolver`` (include/lightfem/solver.hpp:89-92)."""
+
+    def __init__(self, device: int = 0, retain_matrix: bool = True):
+        self.device = device
+        self.retain_matrix = retain_matrix
+        self.context: _native.Context | None = None
+
+    def solve(self, model: Model) -> AnalysisResult:
+        if not model.indexed:
+            raise RuntimeError("model must pass validation and sort_and_index before solving")
+        t0 = time.perf_counter()
+        s = model.settings
+        perf = PerformanceReport(reordering=s.reordering)
+        if s.reordering == "rcm":
+            model.index_with_node_order(_native.host_rcm(model.node_ids, model.element_nodes))
+        if self.context is None:
+            self.context = _native.Context(self.device)
+        ctx = self.context
+        upload_model(ctx, model)
+        strategy = "atomic" if s.assembly == "atomic" or s.gpu_assembly == "atomic" else "coloring"
+        ctx.assemble(strategy)
+        ctx.apply_dirichlet()
+        try:
+            u, rep = ctx.solve(solve_options(s))
+        except _native.GpuError as err:
+            raise RuntimeError(_MESSAGES.get(err.code, str(err))) from err
+        report = LinearSolverReport(
+            converged=bool(rep.converged), iterations=rep.iterations, initial_residual=rep.initial_residual,
+            final_residual=rep.final_residual, preconditioner=s.preconditioner, solve_ms=rep.solve_ms,
+            matvec_ms=rep.matvec_ms, matvec_calls=rep.matvec_calls, storage=s.storage,
+            matrix_bytes_per_matvec=rep.matrix_bytes_per_matvec, storage_convert_ms=rep.storage_convert_ms,
+            preconditioner_setup_ms=rep.preconditioner_setup_ms,
+            preconditioner_apply_ms=rep.preconditioner_apply_ms, subdomains=rep.subdomains,
+            capture_ratio=rep.capture_ratio, precision=s.precision, refinements=rep.refinements,
+            true_residual=rep.true_residual, fallback_fp64=bool(rep.fallback_fp64),
+            ic0_breakdowns=rep.ic0_breakdowns,
+            message="converged" if rep.converged else "maximum iterations reached without convergence")
+        if rep.initial_residual <= rep.final_residual and rep.iterations == 0 and rep.converged:
+            report.message = "initial residual satisfies tolerance"
+        if not report.converged:
+            raise RuntimeError("PCG did not converge: " + report.message)
+        reaction = ctx.reactions()
+        tm = ctx.timings()
+        perf.assembly = strategy
+        perf.coloring_count = tm["coloring_count"]
+        perf.pattern_ms = tm["pattern_ms"]
+        perf.assembly_ms = tm["assembly_ms"]
+        perf.boundary_ms = tm["boundary_ms"]
+        perf.postprocess_ms = tm["reactions_ms"]
+        stiffness = None
+        if self.retain_matrix:
+            rp, col, _, _ = ctx.download_pattern()
+            stiffness = CsrMatrix(rp, col, ctx.download(_native.K_FULL))
+        load = ctx.download(_native.F_FULL)
+        perf.total_ms = (time.perf_counter() - t0) * 1e3
+        return AnalysisResult(stiffness=stiffness, load=load, displacement=u, reaction=reaction, solver=report,
+                              performance=perf)

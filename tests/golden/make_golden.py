@@ -1,0 +1,223 @@
+"""Regenerate the golden fixtures from the reference's own sources.
+
+Run from the repository root in a container where the reference tree is mounted:
+
+    make -C oracle ref          # builds oracle/_ref/ref_dump from the reference sources
+    python tests/golden/make_golden.py
+
+Each case writes a small model through ``lightfem_gb300.mesh.to_fem``, runs
+``oracle/_ref/ref_dump`` on it (the reference's parser, validator, assembly, Dirichlet,
+preconditioners and PCG, see oracle/ref_dump.cpp) and stores the arrays in
+``tests/golden/<case>.npz`` and the scalar reports in ``tests/golden/golden.json``.
+The GPU machine has no reference tree; the tests only read these committed files.
+
+Cases:
+  single_q4  the one-element cantilever of tests/test_solver.cpp:41-62
+  scrambled  the scrambled 2x2 mesh of tests/test_solver.cpp:143-174 (+ RCM)
+  grid6      grid_model(6, 6) of tests/test_solver.cpp:371-396, every iterative variant
+  beam       24x12 perturbed two-material beam: gravity + top pressure, colouring
+  strain     16x8 plane-strain cantilever with RCM (the 1000x1000 workload's physics)
+  adjoint    20x20 cantilever with log-normal per-element moduli + reference FD
+  cfg1       the 200x200 workload: iteration counts, residuals, sampled u and R
+  cfg2       the 1000x1000 workload: known answers from the reference (optional,
+             read from _work/big/cfg2_<variant> when those long runs exist)
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from lightfem_gb300 import mesh  # noqa: E402
+from lightfem_gb300.model import PLANE_STRAIN, Model, SolverSettings  # noqa: E402
+
+REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+OUT = os.path.join(ROOT, "tests", "golden")
+
+
+def run(model: Model, *args: str) -> tuple[dict, dict]:
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "m.fem")
+        with open(path, "w") as fh:
+            fh.write(mesh.to_fem(model, os.path.join(tmp, "out.vtk")))
+        subprocess.run([REF_DUMP, path, tmp, *args], check=True)
+        arrays = {f[:-4]: np.load(os.path.join(tmp, f)) for f in os.listdir(tmp) if f.endswith(".npy")}
+        with open(os.path.join(tmp, "report.json")) as fh:
+            report = json.load(fh)
+    return arrays, report
+
+
+def single_q4() -> Model:
+    return Model(
+        node_ids=np.array([1, 2, 3, 4]), xy=np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [0.0, 1.0]]),
+        material_ids=np.array([1]), young=np.array([1.0e6]), poisson=np.array([0.25]), thickness=np.array([1.0]),
+        element_ids=np.array([1]), element_nodes=np.array([[1, 2, 3, 4]]), element_material=np.array([1]),
+        bc_node=np.array([1, 4]), bc_ux=np.zeros(2), bc_uy=np.zeros(2),
+        load_node=np.array([2]), load_fx=np.zeros(1), load_fy=np.array([-1.0]),
+        settings=SolverSettings(tolerance=1e-12, max_iterations=100))
+
+
+def scrambled() -> Model:
+    ids = np.array([1, 9, 3, 8, 2, 7, 4, 6, 5])
+    xy = np.array([[0, 0], [1, 0], [2, 0], [0, 1], [1, 1], [2, 1], [0, 2], [1, 2], [2, 2]], dtype=float)
+    return Model(
+        node_ids=ids, xy=xy, material_ids=np.array([1]), young=np.array([1.0e6]), poisson=np.array([0.25]),
+        thickness=np.array([1.0]), element_ids=np.array([1, 2, 3, 4]),
+        element_nodes=np.array([[1, 9, 2, 8], [9, 3, 7, 2], [8, 2, 6, 4], [2, 7, 5, 6]]),
+        element_material=np.ones(4, np.int64), bc_node=np.array([1, 4]), bc_ux=np.zeros(2), bc_uy=np.zeros(2),
+        load_node=np.array([3, 5]), load_fx=np.zeros(2), load_fy=np.array([-1.0, -1.0]),
+        settings=SolverSettings(tolerance=1e-12, max_iterations=200))
+
+
+def grid6() -> Model:
+    m = mesh.cantilever(6, 6, length=1.0, height=1.0, young=1.0e6, poisson=0.25, thickness=1.0,
+                        total_load=-0.01 * 7, settings=SolverSettings(tolerance=1e-12, max_iterations=5000))
+    m.load_fy[:] = -0.01
+    return m
+
+
+VARIANTS = {
+    "csr_jacobi": ("storage=csr", "preconditioner=jacobi"),
+    "bsr_jacobi": ("storage=bsr", "preconditioner=jacobi"),
+    "csr_ic0": ("storage=csr", "preconditioner=ic0"),
+    "bsr_ic0": ("storage=bsr", "preconditioner=ic0"),
+    "bsr_block1": ("storage=bsr", "preconditioner=block", "subdomain_split=chunk", "subdomain_nodes=1"),
+    "csr_block1": ("storage=csr", "preconditioner=block", "subdomain_split=chunk", "subdomain_nodes=1"),
+    "bsr_block_rcb2": ("storage=bsr", "preconditioner=block", "subdomain_split=rcb", "subdomain_nodes=2"),
+    "bsr_block_chunk4": ("storage=bsr", "preconditioner=block", "subdomain_split=chunk", "subdomain_nodes=4"),
+}
+
+
+def save(name: str, arrays: dict) -> None:
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **arrays)
+
+
+def main() -> None:
+    if not os.path.exists(REF_DUMP):
+        raise SystemExit("build the reference first: make -C oracle ref")
+    golden: dict = {}
+
+    # --- single Q4 and scrambled mesh: every stage, serial and colouring assembly
+    for name, model in (("single_q4", single_q4()), ("scrambled", scrambled())):
+        arrays, report = run(model, "pattern=1", "ke=4", "precond=1", "subdomain_split=chunk",
+                             "subdomain_nodes=1", "solve=1")
+        col_arrays, col_report = run(model, "pattern=1", "assembly=coloring", "solve=1")
+        arrays["K_coloring"] = col_arrays["K"]
+        arrays["u_coloring"] = col_arrays["u"]
+        report["coloring"] = col_report
+        if name == "scrambled":
+            rcm_arrays, rcm_report = run(model, "pattern=1", "reordering=rcm", "solve=1")
+            for k in ("node_order", "rowptr", "col", "map", "K", "Kc", "fc", "u", "R", "colors"):
+                arrays[f"rcm_{k}"] = rcm_arrays[k]
+            report["rcm"] = rcm_report
+        save(name, arrays)
+        golden[name] = report
+
+    # --- grid6: all iterative variants of tests/test_solver.cpp:398-448
+    model = grid6()
+    arrays, report = run(model, "pattern=1", "ke=2", "precond=1", "subdomain_split=rcb", "subdomain_nodes=2")
+    golden["grid6"] = {"pattern": report}
+    _, r_chunk = run(model, "precond=1", "subdomain_split=chunk", "subdomain_nodes=1")
+    chunk_arrays, _ = run(model, "precond=1", "subdomain_split=chunk", "subdomain_nodes=1")
+    arrays["z_block1"] = chunk_arrays["z_block"]
+    golden["grid6"]["precond_chunk1"] = r_chunk
+    for vname, opts in VARIANTS.items():
+        va, vr = run(model, "solve=1", *opts)
+        arrays[f"u_{vname}"] = va["u"]
+        arrays[f"R_{vname}"] = va["R"]
+        golden["grid6"][vname] = vr
+    save("grid6", arrays)
+
+    # --- perturbed two-material beam with gravity and pressure
+    model = mesh.perturbed_beam(24, 12, seed=7, settings=SolverSettings(
+        tolerance=1e-10, max_iterations=20000, assembly="coloring"))
+    arrays, report = run(model, "pattern=1", "ke=4", "precond=1", "subdomain_split=chunk", "subdomain_nodes=1")
+    golden["beam"] = {"pattern": report}
+    for vname in ("csr_jacobi", "bsr_jacobi", "csr_ic0", "bsr_block1"):
+        va, vr = run(model, "solve=1", *VARIANTS[vname])
+        arrays[f"u_{vname}"] = va["u"]
+        arrays[f"R_{vname}"] = va["R"]
+        golden["beam"][vname] = vr
+    save("beam", arrays)
+
+    # --- plane strain + RCM
+    model = mesh.cantilever(16, 8, young=70e9, poisson=0.33, plane_mode=PLANE_STRAIN,
+                            settings=SolverSettings(tolerance=1e-10, max_iterations=20000, assembly="coloring",
+                                                    reordering="rcm"))
+    arrays, report = run(model, "pattern=1", "ke=2", "precond=1", "subdomain_split=chunk", "subdomain_nodes=1")
+    golden["strain"] = {"pattern": report}
+    for vname in ("csr_jacobi", "csr_ic0", "bsr_block1"):
+        va, vr = run(model, "solve=1", *VARIANTS[vname])
+        arrays[f"u_{vname}"] = va["u"]
+        arrays[f"R_{vname}"] = va["R"]
+        golden["strain"][vname] = vr
+    save("strain", arrays)
+
+    # --- adjoint: log-normal moduli, compliance and tip uy by central differences
+    n = 20
+    model = mesh.cantilever(n, n, poisson=0.3, per_element_young=mesh.lognormal_moduli(n * n, seed=11),
+                            settings=SolverSettings(tolerance=1e-13, max_iterations=50000))
+    tip = mesh.tip_node_id(model)
+    rng = np.random.default_rng(5)
+    elems = np.sort(rng.choice(n * n, size=16, replace=False))
+    arrays, report = run(model, "solve=1", "fd=" + ",".join(str(int(e)) for e in elems), "fd_step=1e-6",
+                         f"tip_node={tip}")
+    report["tip_node"] = tip
+    golden["adjoint"] = report
+    save("adjoint", arrays)
+
+    # --- the 200x200 workload: iteration counts and sampled fields
+    model = mesh.workload(1)
+    arrays, report = run(model, "pattern=1")
+    keep = {"rowptr_sum": np.array([arrays["rowptr"].sum()]), "col_sum": np.array([arrays["col"].sum()]),
+            "map_sum": np.array([arrays["map"].sum()]), "K_sample": arrays["K"][::997],
+            "Kc_sample": arrays["Kc"][::997], "fc": arrays["fc"], "colors": arrays["colors"]}
+    golden["cfg1"] = {"pattern": report, "nnz": int(arrays["col"].shape[0])}
+    for vname in ("csr_jacobi", "bsr_jacobi", "csr_ic0", "bsr_block1"):
+        va, vr = run(model, "solve=1", *VARIANTS[vname])
+        keep[f"u_{vname}"] = va["u"][::101]
+        keep[f"R_{vname}"] = va["R"][::101]
+        vr["u_norm"] = float(np.linalg.norm(va["u"]))
+        vr["R_norm"] = float(np.linalg.norm(va["R"]))
+        golden["cfg1"][vname] = vr
+    save("cfg1", keep)
+
+    # --- the 1000x1000 workload (long runs, made separately)
+    big = os.path.join(ROOT, "_work", "big")
+    cfg2 = {}
+    keep = {}
+    for vname in ("jacobi", "block", "ic0"):
+        d = os.path.join(big, f"cfg2_{vname}")
+        if os.path.exists(os.path.join(d, "report.json")):
+            with open(os.path.join(d, "report.json")) as fh:
+                rep = json.load(fh)
+            u = np.load(os.path.join(d, "u.npy"))
+            r = np.load(os.path.join(d, "R.npy"))
+            rep["u_norm"] = float(np.linalg.norm(u))
+            rep["R_norm"] = float(np.linalg.norm(r))
+            rep["R_y_sum"] = float(r[1::2].sum())
+            cfg2[vname] = rep
+            keep[f"u_{vname}"] = u[::2003]
+    if cfg2:
+        golden["cfg2"] = cfg2
+        save("cfg2", keep)
+    elif os.path.exists(os.path.join(OUT, "golden.json")):
+        with open(os.path.join(OUT, "golden.json")) as fh:
+            old = json.load(fh)
+        if "cfg2" in old:
+            golden["cfg2"] = old["cfg2"]
+
+    with open(os.path.join(OUT, "golden.json"), "w") as fh:
+        json.dump(golden, fh, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

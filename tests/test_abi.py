@@ -1,0 +1,59 @@
+"""The C ABI library loads and exports every entry point include/lfgpu.h declares;
+host-only entry points work without a GPU.  CPU only: no compute call needs CUDA."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from cases import CASES, indexed
+from conftest import ROOT, load_golden
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "lfgpu.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(lfgpu_\w+)\s*\(", text, re.M)))
+
+
+def test_header_and_binding_agree(native):
+    declared = declared_functions()
+    assert len(declared) >= 20
+    assert set(declared) == set(native.EXPORTED)
+
+
+def test_library_exports_every_declared_symbol(native):
+    lib = ctypes.CDLL(native.LIB_PATH)
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    assert native.library().lfgpu_version().decode().startswith("lfgpu")
+
+
+def test_host_rcm_matches_reference(native):
+    for name in ("strain",):
+        g = load_golden(name)
+        model = indexed(CASES[name]())
+        order = native.host_rcm(model.node_ids, model.element_nodes)
+        np.testing.assert_array_equal(order, g["node_order"])
+    g = load_golden("scrambled")
+    model = indexed(CASES["scrambled"]())
+    np.testing.assert_array_equal(native.host_rcm(model.node_ids, model.element_nodes), g["rcm_node_order"])
+
+
+def test_host_rcm_rejects_unknown_node(native):
+    import pytest
+    with pytest.raises(native.GpuError):
+        native.host_rcm(np.array([1, 2, 3, 4]), np.array([[1, 2, 3, 99]]))
+
+
+def test_create_without_gpu_fails_cleanly(native):
+    """Without a visible device the handle refuses to open (no silent fallback)."""
+    import pytest
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is visible")
+    except ImportError:
+        pass
+    with pytest.raises(native.GpuError):
+        native.Context(0)

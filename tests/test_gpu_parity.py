@@ -1,0 +1,231 @@
+"""Parity of the CUDA path (through the C ABI) with the reference's golden vectors and
+with the CPU oracle.
+
+Bars: pattern, map and colours bit-exact; assembled and eliminated values within
+1e-12 of max|K| (summation order differs); displacements and reactions within 1e-8
+relative (2-norm) with PCG iteration counts within 2; mixed precision reaches the
+FP64 true-residual target.
+"""
+
+import numpy as np
+import pytest
+
+from cases import CASES, VARIANTS, adjoint_model, by_id_order, indexed
+from conftest import load_golden
+from lightfem_gb300 import mesh
+from lightfem_gb300.solver import LinearElasticSolver, upload_model
+
+pytestmark = pytest.mark.gpu
+
+GPU_VARIANTS = ["csr_jacobi", "bsr_jacobi", "bsr_block1", "csr_block1"]
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+def prepared(native, name):
+    model = indexed(CASES[name]())
+    if model.settings.reordering == "rcm":
+        model.index_with_node_order(native.host_rcm(model.node_ids, model.element_nodes))
+    ctx = native.Context(0)
+    upload_model(ctx, model)
+    return model, ctx
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_pattern_map_colors_bit_exact(native, name):
+    g = load_golden(name)
+    model, ctx = prepared(native, name)
+    np.testing.assert_array_equal(model.node_ids, g["node_order"])
+    rp, col, mp, colors = ctx.download_pattern()
+    np.testing.assert_array_equal(rp, g["rowptr"])
+    np.testing.assert_array_equal(col, g["col"])
+    np.testing.assert_array_equal(mp, g["map"])
+    np.testing.assert_array_equal(colors, g["colors"])
+
+
+@pytest.mark.parametrize("strategy", ["coloring", "atomic"])
+@pytest.mark.parametrize("name", list(CASES))
+def test_assembly_and_dirichlet(native, name, strategy):
+    g = load_golden(name)
+    model, ctx = prepared(native, name)
+    ctx.assemble(strategy)
+    K = ctx.download(native.K_FULL)
+    f = ctx.download(native.F_FULL)
+    kmax = np.abs(g["K"]).max()
+    assert np.abs(K - g["K"]).max() <= 1e-12 * kmax
+    assert np.abs(f - g["f"]).max() <= 1e-12 * max(np.abs(g["f"]).max(), 1e-300)
+    ctx.apply_dirichlet()
+    Kc = ctx.download(native.K_CONSTRAINED)
+    fc = ctx.download(native.F_CONSTRAINED)
+    assert np.abs(Kc - g["Kc"]).max() <= 1e-12 * kmax
+    assert np.abs(fc - g["fc"]).max() <= 1e-12 * max(np.abs(g["fc"]).max(), 1e-300)
+    eliminated = (g["Kc"] == 0) & (g["K"] != 0)
+    assert np.all(Kc[eliminated] == 0.0)
+    np.testing.assert_array_equal(ctx.download(native.K_FULL), K)
+
+
+def test_element_stiffness_matches_reference(native):
+    """Single-element models against q4_stiffness of the reference (golden Ke)."""
+    for name in ("beam", "strain"):
+        g = load_golden(name)
+        model = indexed(CASES[name]())
+        if model.settings.reordering == "rcm":
+            model.index_with_node_order(native.host_rcm(model.node_ids, model.element_nodes))
+        en = model.element_node_index()
+        mi = model.material_index(model.element_material)
+        for e in range(g["Ke"].shape[0]):
+            ctx = native.Context(0)
+            ctx.set_mesh(model.xy[en[e]], np.arange(4)[None, :], [0], [model.young[mi[e]]],
+                         [model.poisson[mi[e]]], [model.thickness[mi[e]]], model.settings.plane_mode)
+            ctx.build_pattern()
+            ctx.assemble("coloring")
+            K = ctx.download(native.K_FULL).reshape(8, 8)
+            ref = g["Ke"][e].reshape(8, 8)
+            assert np.abs(K - ref).max() <= 1e-12 * np.abs(ref).max()
+            ctx.close()
+
+
+@pytest.mark.parametrize("variant", GPU_VARIANTS)
+@pytest.mark.parametrize("name", ["grid6", "beam", "strain"])
+def test_pcg_fp64_matches_reference(native, golden_json, name, variant):
+    if variant not in golden_json[name]:
+        pytest.skip("variant not in the golden set")
+    g = load_golden(name)
+    storage, precond, _, _ = VARIANTS[variant]
+    model = indexed(CASES[name]())
+    model.settings.storage, model.settings.preconditioner = storage, precond
+    res = LinearElasticSolver().solve(model)
+    ref = golden_json[name][variant]
+    assert abs(res.solver.iterations - ref["iterations"]) <= 2
+    assert rel(by_id_order(model, res.displacement), g[f"u_{variant}"]) <= 1e-8
+    assert rel(by_id_order(model, res.reaction), g[f"R_{variant}"]) <= 1e-8
+    assert res.solver.initial_residual == pytest.approx(ref["initial_residual"], rel=1e-12)
+
+
+@pytest.mark.parametrize("name", ["single_q4", "scrambled"])
+def test_reference_fixture_solves(native, golden_json, name):
+    """tests/test_solver.cpp:106-141 (single Q4: 8 DOFs, nnz 64, sum R_y = 1, fixed
+    DOFs exact) and :176-231 (scrambled mesh, RCM and assembly strategies agree)."""
+    g = load_golden(name)
+    for strategy in ("coloring", "atomic"):
+        model = indexed(CASES[name]())
+        model.settings.assembly = strategy
+        res = LinearElasticSolver().solve(model)
+        u = by_id_order(model, res.displacement)
+        assert np.abs(u - g["u"]).max() <= 1e-11 * max(np.abs(g["u"]).max(), 1.0)
+        if name == "single_q4":
+            assert res.stiffness.nonzeros() == 64 and res.displacement.shape[0] == 8
+            assert abs(res.reaction[1::2].sum() - 1.0) <= 1e-10
+            assert np.all(np.abs(res.displacement[[0, 1, 6, 7]]) <= 1e-14)
+        if name == "scrambled":
+            m2 = indexed(CASES[name]())
+            m2.settings.reordering = "rcm"
+            r2 = LinearElasticSolver().solve(m2)
+            assert np.abs(by_id_order(m2, r2.displacement) - u).max() <= 1e-13
+
+
+def test_cfg1_full_size(native, golden_json):
+    """The 200x200 workload against the reference's iteration counts and fields."""
+    g = load_golden("cfg1")
+    ref = golden_json["cfg1"]
+    for variant in ("csr_jacobi", "bsr_jacobi", "bsr_block1"):
+        storage, precond, _, _ = VARIANTS[variant]
+        model = indexed(mesh.workload(1))
+        model.settings.storage, model.settings.preconditioner = storage, precond
+        res = LinearElasticSolver(retain_matrix=False).solve(model)
+        assert abs(res.solver.iterations - ref[variant]["iterations"]) <= 2, variant
+        assert rel(res.displacement[::101], g[f"u_{variant}"]) <= 1e-8, variant
+        assert rel(res.reaction[::101], g[f"R_{variant}"]) <= 1e-8, variant
+        assert abs(res.reaction[1::2].sum() + 1000.0) <= 1e-6
+        assert res.solver.true_residual <= 1.01e-8 * ref[variant]["initial_residual"]
+
+
+@pytest.mark.parametrize("storage", ["csr", "bsr"])
+@pytest.mark.parametrize("precond", ["jacobi", "block"])
+@pytest.mark.parametrize("refinement", ["reliable", "restart"])
+def test_mixed_precision_reaches_fp64_target(native, storage, precond, refinement):
+    model = indexed(mesh.workload(1, scale=4))
+    model.settings.storage, model.settings.preconditioner = storage, precond
+    fp64 = LinearElasticSolver().solve(model.copy())
+    model.settings.precision, model.settings.refinement = "mixed", refinement
+    res = LinearElasticSolver().solve(model)
+    tol = model.settings.tolerance * res.solver.initial_residual
+    assert res.solver.converged
+    assert res.solver.true_residual <= 1.001 * tol
+    assert res.solver.final_residual <= tol
+    assert res.solver.refinements >= 1
+    # Two solutions at a 1e-8 relative residual differ by at most cond(K) * 1e-8;
+    # the FP64 solution is the oracle here.
+    assert rel(res.displacement, fp64.displacement) <= 1e-4
+
+
+def test_spmv_products(native, oracle):
+    model, ctx = prepared(native, "beam")
+    ctx.assemble("coloring")
+    ctx.apply_dirichlet()
+    Kc = ctx.download(native.K_CONSTRAINED)
+    rp, col, _, _ = ctx.download_pattern()
+    x = np.random.default_rng(3).standard_normal(model.n_dofs)
+    y_ref = oracle.spmv(rp, col, Kc, x)
+    scale = np.abs(y_ref).max()
+    for storage in ("csr", "bsr"):
+        y, _ = ctx.spmv(x, which=1, storage=storage, precision="fp64")
+        assert np.abs(y - y_ref).max() <= 1e-13 * scale
+        y32, _ = ctx.spmv(x, which=1, storage=storage, precision="mixed")
+        assert np.abs(y32 - y_ref).max() <= 1e-5 * scale
+
+
+def test_adjoint_gradients(native, oracle, golden_json):
+    g = load_golden("adjoint")
+    ref = golden_json["adjoint"]
+    model = indexed(adjoint_model())
+    solver = LinearElasticSolver()
+    res = solver.solve(model)
+    ctx = solver.context
+    grad_c, _ = ctx.adjoint(None)
+    en = model.element_node_index()
+    mi = model.material_index(model.element_material)
+    args = (model.xy, en, model.young[mi], model.poisson[mi], model.thickness[mi], model.settings.plane_mode)
+    u = res.displacement
+    want = oracle.adjoint_grad(*args, u, u)
+    assert np.abs(grad_c - want).max() <= 1e-12 * np.abs(want).max()
+    tip = model.node_index([ref["tip_node"]])[0]
+    dj = np.zeros(model.n_dofs)
+    dj[2 * tip + 1] = 1.0
+    opts = ctx.options(1e-13, 50000)
+    grad_t, rep = ctx.adjoint(dj, opts)
+    assert rep.converged
+    el = g["fd_elements"]
+    np.testing.assert_allclose(grad_c[el], g["fd_dc_dE"], rtol=1e-4)
+    np.testing.assert_allclose(grad_t[el], g["fd_dtip_dE"], rtol=1e-4, atol=1e-4 * np.abs(g["fd_dtip_dE"]).max())
+
+
+def test_errors_map_to_reference_exceptions(native):
+    # Clockwise element: non-positive Jacobian (src/element.cpp:52-54).
+    ctx = native.Context(0)
+    ctx.set_mesh([[0, 0], [0, 1], [1, 1], [1, 0]], [[0, 1, 2, 3]], [0], [1e6], [0.25], [1.0], 0)
+    ctx.build_pattern()
+    with pytest.raises(native.GpuError) as err:
+        ctx.assemble("coloring")
+    assert err.value.code == native.ERR_JACOBIAN and "non-positive Jacobian" in str(err.value)
+    # Negative modulus: the first r.z is negative (src/solver.cpp:579-581).
+    model = indexed(CASES["grid6"]())
+    model.young[:] = -1e6
+    with pytest.raises(RuntimeError, match="positive initial preconditioned residual"):
+        LinearElasticSolver().solve(model)
+    # Iteration cap: reported, then "PCG did not converge" (src/solver.cpp:948-950).
+    model = indexed(CASES["grid6"]())
+    model.settings.max_iterations = 1
+    with pytest.raises(RuntimeError, match="PCG did not converge"):
+        LinearElasticSolver().solve(model)
+    # Bad map index is rejected on the host before any kernel sees it.
+    ctx = native.Context(0)
+    m = indexed(CASES["single_q4"]())
+    upload_model(ctx, m)
+    rp, col, mp, colors = ctx.download_pattern()
+    mp = mp.copy()
+    mp[0, 5] = 10**6
+    with pytest.raises(native.GpuError):
+        ctx.set_pattern(rp, col, mp, colors)
