@@ -1,0 +1,472 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300-native LightFEM solve path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the 1000x1000 Q4 plane-strain cantilever (2,004,002 DOFs, 36,024,004
+nonzeros, RCM ordering), solved to a 1e-8 relative residual.  A step is one pass of
+the solve path on one GPU with the model resident in HBM: element stiffness +
+colouring assembly + loads, Dirichlet elimination, the PCG solve, reactions.
+`value` is the device time of a step (CUDA events on the library's stream) for the
+FP32-inner PCG with FP64 refinement; the FP64 PCG of the same storage and
+preconditioner is timed beside it.  Every input array (K alone is 324 MB in FP64
+BSR) is larger than the 129 MB L2, so no flush is needed between steps.
+
+`e2e` is the same step through the C ABI from pinned host buffers: mesh, pattern,
+element map, colours, loads and constraints are uploaded, and u and R downloaded,
+inside the timed region of every step.
+
+`--impl reference` times the reference's algorithm on the host cores instead (the
+CPU restatement in oracle/, which reproduces the reference's iterates bit for bit),
+on a bounded sample of PCG iterations extrapolated to the reference's own
+iteration count for this model.
+
+Under torchrun each rank solves its own copy of the model on its own GPU (weak
+scaling, no collective on the data path); rank 0 prints the max over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Solve ms to 1e-8 rel. residual, 2M-dof Q4: FP32+refine vs FP64 PCG; SpMV GB/s"
+WORKLOAD = "1000x1000 Q4 plane-strain cantilever (2.0 m x 1.0 m), 2,004,002 DOFs, 36,024,004 nnz, RCM"
+DATA = ("synthetic: seeded structured Q4 mesh of the 1000x1000 cantilever workload (E 70 GPa, nu 0.33, "
+        "t 0.01 m, left edge clamped, -1000 N over the right-edge nodes)")
+CONFIG_IDX = 2
+STEP_DESC = "element stiffness + colouring assembly + loads, Dirichlet, PCG to 1e-8, reactions"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Dist:
+    """Host-side barrier and max-reduction across torchrun ranks (gloo)."""
+
+    def __init__(self, world: int):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.dist:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.index = gpu_index
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9 or not f[0].isdigit() or int(f[0]) != self.index:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def gpu_index_for(local_rank: int) -> int:
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    ids = [v for v in vis.split(",") if v.strip()]
+    if ids and ids[min(local_rank, len(ids) - 1)].strip().isdigit():
+        return int(ids[min(local_rank, len(ids) - 1)])
+    return local_rank
+
+
+# ---------------------------------------------------------------------- model
+def build_model(scale: int = 1):
+    from lightfem_gb300 import mesh
+    m = mesh.workload(CONFIG_IDX, scale=scale)
+    m.sort_and_index()
+    return m
+
+
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profiled_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        for line in fh:
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel:
+                try:
+                    return float(parts[1])
+                except ValueError:
+                    return None
+    return None
+
+
+def spmv_bytes(kind: str, n: int, nnz: int, nblocks: int) -> int:
+    """Algorithmic bytes of one product (int32 columns and row pointers, x read once,
+    y written once): CSR Z(s+4) + 4(n+1) + 2sn, BSR B(4s+4) + 4(n/2+1) + 2sn."""
+    s = 8 if kind.endswith("64") else 4
+    if kind.startswith("csr"):
+        return nnz * (s + 4) + 4 * (n + 1) + 2 * s * n
+    return nblocks * (4 * s + 4) + 4 * (n // 2 + 1) + 2 * s * n
+
+
+# ---------------------------------------------------------------------- CPU leg
+def reference_iterations(storage: str, precond: str) -> tuple[int, str]:
+    """The reference's own PCG iteration count on this model (tests/golden/golden.json)."""
+    with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as fh:
+        g = json.load(fh).get("cfg2", {})
+    key = {("bsr", "jacobi"): "bsr_jacobi", ("csr", "jacobi"): "jacobi", ("bsr", "block"): "block",
+           ("csr", "ic0"): "ic0"}.get((storage, precond), "jacobi")
+    if key in g:
+        return int(g[key]["iterations"]), key
+    return int(g["jacobi"]["iterations"]), "jacobi"
+
+
+def cpu_solve_sample(model, storage: str, precond: str, sample_iters: int, threads: int = 0) -> dict:
+    """Time the reference algorithm (oracle restatement) on the host: assembly,
+    elimination, preconditioner setup, `sample_iters` PCG iterations and the
+    reactions product; the PCG time is extrapolated to the reference's iteration
+    count for this model.  TEST/BASELINE INFRASTRUCTURE: this is the only place
+    bench.py runs the oracle."""
+    from oracle import lf_oracle as O
+    if threads > 0:
+        O.set_threads(threads)
+    m = model.copy()
+    t0 = time.perf_counter()
+    out = O.solve_model(m, stop_after="dirichlet", assembly="coloring")
+    setup_total = (time.perf_counter() - t0) * 1e3
+    asm_ms = out["timing"]["assembly_ms"]
+    bnd_ms = out["timing"]["boundary_ms"]
+    t1 = time.perf_counter()
+    u, rep = O.pcg(out["rowptr"], out["col"], out["Kc"], out["fc"], 1e-8, 10 ** 6, storage, precond, "chunk", 1,
+                   m.xy, iteration_cap=sample_iters)
+    pcg_total = (time.perf_counter() - t1) * 1e3
+    t2 = time.perf_counter()
+    O.spmv(out["rowptr"], out["col"], out["K"], u)
+    react_ms = (time.perf_counter() - t2) * 1e3
+    iters = max(1, rep["iterations"])
+    per_iter = rep["solve_ms"] / iters
+    outside_loop = pcg_total - rep["solve_ms"]  # BSR conversion + preconditioner setup
+    full_iters, key = reference_iterations(storage, precond)
+    value = asm_ms + bnd_ms + outside_loop + per_iter * full_iters + react_ms
+    return {"value": value, "per_iter_ms": per_iter, "sample_iters": iters, "full_iters": full_iters,
+            "iters_source": f"reference run on this model ({key})", "assembly_ms": asm_ms, "boundary_ms": bnd_ms,
+            "pcg_setup_ms": outside_loop, "reactions_ms": react_ms, "threads": O.num_threads(),
+            "untimed_setup_ms": setup_total - asm_ms - bnd_ms}
+
+
+def run_reference(args) -> int:
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    model = build_model(args.scale)
+    storage, precond = args.storage, args.precond if args.precond != "block" else "block"
+    values = []
+    last = None
+    for k in range(args.warmup + args.steps):
+        r = cpu_solve_sample(model, storage, precond, args.ref_sample_iters)
+        if k >= args.warmup:
+            values.append(r["value"])
+        last = r
+        log(f"reference step {k}: {r['value']:.1f} ms (per-iteration {r['per_iter_ms']:.3f} ms)")
+    value = statistics.median(values) if values else last["value"]
+    sample = (f"{last['sample_iters']} PCG iterations per step ({storage}/{precond}, FP64) plus full assembly, "
+              f"elimination, setup and reactions; loop time extrapolated to the reference's {last['full_iters']} "
+              f"iterations")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "ms", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": {"workload": WORKLOAD, "precision": "fp64", "storage": storage, "preconditioner": precond,
+                   "tolerance": 1e-8, "step": STEP_DESC},
+        "cpu_baseline": {"value": round(value, 3), "unit": "ms", "cores": last["threads"], "kind": "port",
+                         "sample": sample, "per_iter_ms": round(last["per_iter_ms"], 4)},
+        "e2e": {"value": round(value, 3), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------- GPU leg
+_PINNED = []
+
+
+def pinned(a: np.ndarray) -> np.ndarray:
+    """A copy of `a` in page-locked host memory (torch only allocates it)."""
+    try:
+        import torch
+        t = torch.empty(a.size, dtype={np.dtype(np.float64): torch.float64, np.dtype(np.int32): torch.int32,
+                                       np.dtype(np.int64): torch.int64}[a.dtype], pin_memory=True)
+        _PINNED.append(t)  # the numpy view below does not own the allocation
+        out = t.numpy().reshape(a.shape)
+        out[...] = a
+        return out
+    except Exception:
+        return np.ascontiguousarray(a)
+
+
+def run_ours(args) -> int:
+    from lightfem_gb300 import _native
+    from lightfem_gb300.solver import upload_model
+
+    world, rank, local = dist_env()
+    dist = Dist(world)
+    model = build_model(args.scale)
+    model.index_with_node_order(_native.host_rcm(model.node_ids, model.element_nodes))
+    ctx = _native.Context(local)
+    upload_model(ctx, model)
+    n, nnz = ctx.n_dofs, ctx.nnz
+    nblocks = nnz // 4
+    tol = 1e-8
+
+    def opts(precision, storage=args.storage, precond=args.precond, persistent=False):
+        return ctx.options(tol, 200000, storage, precond, precision, "reliable", persistent=persistent)
+
+    def step(o):
+        ctx.event_record(0)
+        ctx.assemble("coloring")
+        ctx.apply_dirichlet()
+        _, rep = ctx.solve(o, download=False)
+        ctx.reactions(download=False)
+        ctx.event_record(1)
+        return ctx.event_elapsed(0, 1), rep
+
+    main = opts("mixed")
+    if args.profile_iters:
+        # Profiling run (not a benchmark): one step with the PCG capped at
+        # --profile-iters iterations, then three standalone products of each kind.
+        capped = ctx.options(tol, args.profile_iters, args.storage, args.precond, "mixed", "reliable")
+        ms, rep = step(capped)
+        x = np.random.default_rng(0).standard_normal(n)
+        for st in ("csr", "bsr"):
+            for prec in ("fp64", "mixed"):
+                ctx.spmv(x, 1, st, prec, repeat=3)
+        print(json.dumps({"profile_iters": args.profile_iters, "step_ms": ms, "iterations": rep.iterations}))
+        ctx.close()
+        return 0
+    for _ in range(args.warmup):
+        step(main)
+    dist.barrier()
+    launches0 = ctx.timings()["kernel_launches"]
+    sampler = ClockSampler(gpu_index_for(local))
+    times, reps = [], []
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        ms, rep = step(main)
+        times.append(ms)
+        reps.append(rep)
+    wall = time.perf_counter() - t_wall
+    clocks = sampler.stop()
+    launches = ctx.timings()["kernel_launches"] - launches0
+    dist.barrier()
+    ms_step = dist.max(statistics.mean(times))
+    rep = reps[-1]
+    u = ctx.download(_native.U)
+    R = ctx.reactions()
+    true_rel = rep.true_residual / rep.initial_residual
+
+    # FP64 PCG of the same storage and preconditioner
+    fp64_times, fp64_rep = [], None
+    for k in range(max(1, args.fp64_steps) + 1):
+        ms, fp64_rep = step(opts("fp64"))
+        if k > 0:
+            fp64_times.append(ms)
+    u64 = ctx.download(_native.U)
+    fp64_ms = dist.max(statistics.mean(fp64_times))
+
+    # other variants, one solve each (device time of the solve alone)
+    variants = []
+    for prec, st, pc, pers in (("mixed", "bsr", "block", False), ("mixed", "csr", "jacobi", False),
+                               ("fp64", "csr", "jacobi", False), ("fp64", "bsr", "block", False),
+                               ("mixed", "bsr", "jacobi", True), ("fp64", "csr", "jacobi", True)):
+        try:
+            ms, r = step(opts(prec, st, pc, pers))
+            variants.append({"precision": prec, "storage": st, "preconditioner": pc,
+                             "loop": "persistent" if pers else "graph", "step_ms": round(ms, 2),
+                             "solve_ms": round(r.solve_ms, 2), "iterations": r.iterations,
+                             "refinements": r.refinements, "true_residual_rel": r.true_residual / r.initial_residual})
+        except _native.GpuError as e:
+            variants.append({"precision": prec, "storage": st, "preconditioner": pc, "error": str(e)})
+    ctx.assemble("coloring")
+    ctx.apply_dirichlet()
+
+    # products: standalone launches, device-timed over 20 calls each
+    x = np.random.default_rng(0).standard_normal(n)
+    spmv = {}
+    for st in ("csr", "bsr"):
+        for prec, tag in (("fp64", "64"), ("mixed", "32")):
+            _, ms = ctx.spmv(x, 1, st, prec, repeat=20)
+            b = spmv_bytes(st + tag, n, nnz, nblocks)
+            spmv[f"{st}{tag}"] = {"us": round(ms * 1e3, 2), "algorithmic_bytes": b, "gbs": round(b / ms / 1e6, 1)}
+
+    # roofline of the dominant kernel: the FP32 product of the inner solve
+    peaks = measured_peaks()
+    dom_key = f"{args.storage}32"
+    dom = spmv[dom_key]
+    achieved = dom["gbs"]
+    kernel_name = "spmv_bsr32_kernel" if args.storage == "bsr" else "spmv_csr_kernel<float>"
+    traffic = profiled_traffic(kernel_name)
+    roofline = {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 3), "traffic": traffic,
+                "algorithmic_bytes": dom["algorithmic_bytes"], "peak_source": peaks["source"]}
+
+    # end to end through the C ABI from pinned host buffers
+    rp, col, mp, colors = ctx.download_pattern()
+    en = model.element_node_index().astype(np.int32)
+    em = model.material_index(model.element_material).astype(np.int32)
+    cd, cv = model.constraints()
+    host = {"xy": pinned(np.ascontiguousarray(model.xy)), "en": pinned(en), "em": pinned(em),
+            "young": pinned(model.young.copy()), "nu": pinned(model.poisson.copy()),
+            "t": pinned(model.thickness.copy()), "rp": pinned(rp), "col": pinned(col), "map": pinned(mp),
+            "colors": pinned(colors), "f": pinned(model.nodal_load_vector()), "cd": pinned(cd), "cv": pinned(cv)}
+    h2d = sum(int(a.nbytes) for a in host.values())
+    e2e_times = []
+    for k in range(args.e2e_steps + 1):
+        ctx.event_record(2)
+        ctx.set_mesh(host["xy"], host["en"], host["em"], host["young"], host["nu"], host["t"],
+                     model.settings.plane_mode)
+        ctx.set_pattern(host["rp"], host["col"], host["map"], host["colors"])
+        ctx.set_loads(host["f"])
+        ctx.set_constraints(host["cd"], host["cv"])
+        ctx.assemble("coloring")
+        ctx.apply_dirichlet()
+        u_e2e, _ = ctx.solve(main, download=True)
+        r_e2e = ctx.reactions(download=True)
+        ctx.event_record(3)
+        if k > 0:
+            e2e_times.append(ctx.event_elapsed(2, 3))
+    d2h = int(u_e2e.nbytes + r_e2e.nbytes)
+    e2e_ms = dist.max(statistics.mean(e2e_times))
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_solve_sample(model, args.storage, args.precond if args.precond != "block" else "block",
+                               args.cpu_sample_iters)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(ms_step, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": DATA,
+            "config": {"workload": WORKLOAD, "precision": "mixed (FP32 inner PCG, FP64 refinement)",
+                       "storage": args.storage, "preconditioner": args.precond, "tolerance": tol,
+                       "step": STEP_DESC, "loop": "device-driven CUDA graph (conditional WHILE)",
+                       "l2": "inputs larger than L2 (K: 324 MB FP64 BSR, 180 MB FP32 BSR)"},
+            "iterations": rep.iterations, "refinements": rep.refinements, "true_residual_rel": true_rel,
+            "solve_ms": round(rep.solve_ms, 3),
+            "fp64": {"step_ms": round(fp64_ms, 3), "iterations": fp64_rep.iterations,
+                     "true_residual_rel": fp64_rep.true_residual / fp64_rep.initial_residual,
+                     "solve_ms": round(fp64_rep.solve_ms, 3)},
+            "speedup_mixed_vs_fp64": round(fp64_ms / ms_step, 3),
+            "mixed_vs_fp64_u_rel": float(np.linalg.norm(u - u64) / np.linalg.norm(u64)),
+            "reaction_sum_y": float(R[1::2].sum()),
+            "variants": variants, "spmv": spmv, "roofline": roofline, "clocks": clocks,
+            "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "wall_s_timed": round(wall, 3),
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = {
+                "value": round(cpu["value"], 1), "unit": "ms", "cores": cpu["threads"], "kind": "port",
+                "sample": (f"{cpu['sample_iters']} FP64 PCG iterations ({args.storage}/{args.precond}) plus full "
+                           f"assembly, elimination, setup and reactions, loop extrapolated to the reference's "
+                           f"{cpu['full_iters']} iterations"),
+                "per_iter_ms": round(cpu["per_iter_ms"], 4)}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    dist.close()
+    return 0
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--storage", choices=("csr", "bsr"), default="bsr")
+    ap.add_argument("--precond", choices=("jacobi", "block"), default="jacobi")
+    ap.add_argument("--scale", type=int, default=1, help="divide the mesh size (testing only)")
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-sample-iters", type=int, default=300)
+    ap.add_argument("--ref-sample-iters", type=int, default=300)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-iters", type=int, default=0,
+                    help="profiling run for ncu: one step capped at this many PCG iterations (not a benchmark)")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        log("note: fewer than 3 warm-up steps")
+    return run_reference(args) if args.impl == "reference" else run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

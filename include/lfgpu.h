@@ -89,6 +89,9 @@ typedef struct lfgpu_solve_options {
     int32_t refinement;        /* LFGPU_REFINE_* (mixed only) */
     double inner_reduction;    /* mixed: FP32 residual drop that triggers an FP64 update */
     int64_t max_refinements;   /* mixed: cap on FP64 residual replacements */
+    int32_t persistent;        /* 1: one persistent cooperative kernel; 0: device-driven CUDA graph of
+                                  per-phase kernels (conditional WHILE node) */
+    int32_t reserved;
 } lfgpu_solve_options;
 
 /* Mirrors LinearSolverReport (include/lightfem/solver.hpp:12-34) plus GPU fields. */
@@ -113,6 +116,11 @@ typedef struct lfgpu_report {
     int64_t ic0_breakdowns;          /* ic0: clamped pivots */
     int64_t ic0_levels;              /* ic0: forward + backward level count */
     int64_t fallback_fp64;           /* mixed: 1 if the FP32 inner solve stagnated and FP64 PCG finished */
+    /* Time inside the persistent PCG kernel as CTA 0 sees it, summed over iterations:
+     * [0] product phase, [1] grid sum after it, [2] update phase, [3] grid sum after
+     * it, [4] FP64: p update / mixed: residual replacements, [5] FP64: barrier after
+     * the p update.  matvec_ms equals phase_ms[0]. */
+    double phase_ms[6];
 } lfgpu_report;
 
 /* Stage timings of the last calls (device time, CUDA events), as in PerformanceReport. */
@@ -122,6 +130,7 @@ typedef struct lfgpu_timings {
     double boundary_ms;      /* retain copy + elimination + zero-pivot sweep */
     double reactions_ms;
     int64_t coloring_count;  /* colours used by the colouring strategy */
+    int64_t kernel_launches; /* kernels this handle has launched so far (graph nodes included) */
 } lfgpu_timings;
 
 /* --- handle ------------------------------------------------------------------- */
@@ -181,6 +190,11 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* options, double* u_out, lf
 int lfgpu_reactions(lfgpu_t h, double* r_out);
 int lfgpu_download(lfgpu_t h, int32_t which, double* out);
 int lfgpu_timings_get(lfgpu_t h, lfgpu_timings* out);
+
+/* Device timing across several calls: record event `slot` (0..7) on the handle's
+ * stream, and read the device time between two recorded slots (synchronises). */
+int lfgpu_event_record(lfgpu_t h, int32_t slot);
+int lfgpu_event_elapsed(lfgpu_t h, int32_t slot_a, int32_t slot_b, double* ms);
 
 /* One product y = A x on the device copy of K_CONSTRAINED (which = 1) or K_FULL
  * (which = 0) in the given storage and precision; device-timed over `repeat` calls.

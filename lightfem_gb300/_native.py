@@ -30,7 +30,8 @@ K_FULL, K_CONSTRAINED, F_FULL, F_CONSTRAINED, U, R = range(6)
 class SolveOptions(ctypes.Structure):
     _fields_ = [("tolerance", c_double), ("max_iterations", c_int64), ("storage", c_int32),
                 ("preconditioner", c_int32), ("precision", c_int32), ("refinement", c_int32),
-                ("inner_reduction", c_double), ("max_refinements", c_int64)]
+                ("inner_reduction", c_double), ("max_refinements", c_int64), ("persistent", c_int32),
+                ("reserved", c_int32)]
 
 
 class Report(ctypes.Structure):
@@ -40,15 +41,18 @@ class Report(ctypes.Structure):
                 ("matrix_bytes_per_matvec", c_int64), ("storage_convert_ms", c_double),
                 ("preconditioner_setup_ms", c_double), ("preconditioner_apply_ms", c_double),
                 ("subdomains", c_int64), ("capture_ratio", c_double), ("degenerate_subdomains", c_int64),
-                ("ic0_breakdowns", c_int64), ("ic0_levels", c_int64), ("fallback_fp64", c_int64)]
+                ("ic0_breakdowns", c_int64), ("ic0_levels", c_int64), ("fallback_fp64", c_int64),
+                ("phase_ms", c_double * 6)]
 
     def as_dict(self) -> dict:
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        d = {name: getattr(self, name) for name, _ in self._fields_}
+        d["phase_ms"] = list(self.phase_ms)
+        return d
 
 
 class Timings(ctypes.Structure):
     _fields_ = [("pattern_ms", c_double), ("assembly_ms", c_double), ("boundary_ms", c_double),
-                ("reactions_ms", c_double), ("coloring_count", c_int64)]
+                ("reactions_ms", c_double), ("coloring_count", c_int64), ("kernel_launches", c_int64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -85,6 +89,8 @@ _SIGNATURES = {
     "lfgpu_reactions": (c_int, [c_void_p, c_void_p]),
     "lfgpu_download": (c_int, [c_void_p, c_int32, c_void_p]),
     "lfgpu_timings_get": (c_int, [c_void_p, POINTER(Timings)]),
+    "lfgpu_event_record": (c_int, [c_void_p, c_int32]),
+    "lfgpu_event_elapsed": (c_int, [c_void_p, c_int32, c_int32, POINTER(c_double)]),
     "lfgpu_spmv": (c_int, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, POINTER(c_double)]),
     "lfgpu_adjoint": (c_int, [c_void_p, c_void_p, POINTER(SolveOptions), c_void_p, POINTER(Report)]),
     "lfgpu_host_rcm": (c_int, [c_int64, c_void_p, c_int64, c_void_p, c_void_p]),
@@ -239,10 +245,10 @@ class Context:
     @staticmethod
     def options(tolerance: float, max_iterations: int, storage: str = "csr", preconditioner: str = "jacobi",
                 precision: str = "fp64", refinement: str = "reliable", inner_reduction: float = 0.0,
-                max_refinements: int = 0) -> SolveOptions:
+                max_refinements: int = 0, persistent: bool = False) -> SolveOptions:
         return SolveOptions(float(tolerance), int(max_iterations), STORAGE[storage], PRECOND[preconditioner],
                             PRECISION[precision], REFINEMENT[refinement], float(inner_reduction),
-                            int(max_refinements))
+                            int(max_refinements), int(bool(persistent)), 0)
 
     def solve(self, options: SolveOptions, download: bool = True):
         rep = Report()
@@ -270,6 +276,15 @@ class Context:
         t = Timings()
         self._check(self._lib.lfgpu_timings_get(self._h, ctypes.byref(t)))
         return t.as_dict()
+
+    def event_record(self, slot: int) -> None:
+        """Record event ``slot`` on this handle's stream (device timing across calls)."""
+        self._check(self._lib.lfgpu_event_record(self._h, int(slot)))
+
+    def event_elapsed(self, slot_a: int, slot_b: int) -> float:
+        ms = c_double()
+        self._check(self._lib.lfgpu_event_elapsed(self._h, int(slot_a), int(slot_b), ctypes.byref(ms)))
+        return ms.value
 
     def spmv(self, x, which: int = 1, storage: str = "csr", precision: str = "fp64", repeat: int = 1):
         x = _arr(x, np.float64)

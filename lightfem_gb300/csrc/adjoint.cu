@@ -104,6 +104,7 @@ void launch_adjoint_grad(Context& c, const double* u, const double* lam, double*
     adjoint_grad_kernel<<<grid_for(E, 128), 128, 0, c.stream>>>(
         E, c.xy, c.elem_nodes, c.elem_mat, c.mat_nu, c.mat_t, c.plane_mode == LFGPU_PLANE_STRAIN,
         reinterpret_cast<const double2*>(u), reinterpret_cast<const double2*>(lam), grad, c.status);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
 }
 

@@ -188,9 +188,11 @@ void install_pattern(Context& c, i64 n, i64 nnz, const int64_t* rowptr64, const 
         LF_CUDA(cudaMemsetAsync(c.prescribed.p, 0, sizeof(double) * n, c.stream));
     }
     c.h_rowptr_cache = rp;
+    c.h_brow.clear();
     c.have_pattern = true;
     c.assembled = c.constrained = c.solved = false;
     ++c.k_version;
+    ++c.pattern_version;
     check_status(c);
 }
 
@@ -250,6 +252,8 @@ int lfgpu_destroy(lfgpu_t h) {
     h->bar.release();
     h->status.release();
     h->pcg_result.release();
+    for (auto& ev : h->user_ev)
+        if (ev) cudaEventDestroy(ev);
     if (h->ev_a) cudaEventDestroy(h->ev_a);
     if (h->ev_b) cudaEventDestroy(h->ev_b);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -512,7 +516,7 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
             ensure_preconditioners(*h);
             LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
             r.preconditioner_setup_ms = elapsed_ms(*h);
-            res = run_pcg(*h, s, &ms);
+            res = o->persistent ? run_pcg(*h, s, &ms) : run_cg_graph(*h, s, &ms);
             if (o->preconditioner == LFGPU_PRECOND_BLOCK2) {
                 r.subdomains = h->n / 2;
                 r.capture_ratio = capture_ratio_2x2(*h);
@@ -526,6 +530,8 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
         r.final_residual = res.final_residual;
         r.converged = res.converged;
         r.status = res.status;
+        for (int k = 0; k < 6; ++k) r.phase_ms[k] = static_cast<double>(res.phase_ns[k]) * 1e-6;
+        r.matvec_ms = r.phase_ms[0];
         if (s.mixed && res.stagnated && res.status == LFGPU_OK) {
             // The FP32 inner solve stopped making progress: finish in FP64 from the
             // current solution.
@@ -539,7 +545,7 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
             f.max_iterations = std::max<i64>(1, o->max_iterations - res.iterations);
             float ms2 = 0.f;
             PcgResult r2 = o->preconditioner == LFGPU_PRECOND_IC0 ? run_pcg_ic0(*h, f, &ms2, &apply_ms)
-                                                                  : run_pcg(*h, f, &ms2);
+                                                                  : (o->persistent ? run_pcg(*h, f, &ms2) : run_cg_graph(*h, f, &ms2));
             total_ms += ms2;
             r.iterations += r2.iterations;
             r.final_residual = r2.final_residual;
@@ -634,6 +640,27 @@ int lfgpu_timings_get(lfgpu_t h, lfgpu_timings* out) {
     return guarded(h, [&] {
         LF_REQUIRE(out != nullptr, LFGPU_ERR_ARGUMENT, "null output");
         *out = h->timings;
+        out->kernel_launches = h->launches;
+    });
+}
+
+int lfgpu_event_record(lfgpu_t h, int32_t slot) {
+    return guarded(h, [&] {
+        LF_REQUIRE(slot >= 0 && slot < 8, LFGPU_ERR_ARGUMENT, "event slot must be in [0, 8)");
+        if (!h->user_ev[slot]) LF_CUDA(cudaEventCreate(&h->user_ev[slot]));
+        LF_CUDA(cudaEventRecord(h->user_ev[slot], h->stream));
+    });
+}
+
+int lfgpu_event_elapsed(lfgpu_t h, int32_t slot_a, int32_t slot_b, double* ms) {
+    return guarded(h, [&] {
+        LF_REQUIRE(slot_a >= 0 && slot_a < 8 && slot_b >= 0 && slot_b < 8 && ms, LFGPU_ERR_ARGUMENT,
+                   "bad event slots");
+        LF_REQUIRE(h->user_ev[slot_a] && h->user_ev[slot_b], LFGPU_ERR_STATE, "event slot never recorded");
+        LF_CUDA(cudaEventSynchronize(h->user_ev[slot_b]));
+        float f = 0.f;
+        LF_CUDA(cudaEventElapsedTime(&f, h->user_ev[slot_a], h->user_ev[slot_b]));
+        *ms = f;
     });
 }
 
@@ -746,7 +773,7 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
                 res = run_pcg_ic0(*h, s, &ms, &apply_ms);
             } else {
                 ensure_preconditioners(*h);
-                res = run_pcg(*h, s, &ms);
+                res = o->persistent ? run_pcg(*h, s, &ms) : run_cg_graph(*h, s, &ms);
             }
             adj_rhs.release();
             r.iterations = res.iterations;

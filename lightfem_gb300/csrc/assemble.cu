@@ -261,6 +261,7 @@ void launch_assembly(Context& c, int strategy) {
         a.count = static_cast<int>(c.n_elem);
         if (a.count > 0)
             q4_assemble_kernel<true><<<grid_for(a.count, kAsmThreads), kAsmThreads, 0, c.stream>>>(a);
+            c.launches += 1;
         LF_CUDA(cudaGetLastError());
         return;
     }
@@ -270,6 +271,7 @@ void launch_assembly(Context& c, int strategy) {
         a.elems = c.color_elems.p + lo;
         a.count = hi - lo;
         q4_assemble_kernel<false><<<grid_for(a.count, kAsmThreads), kAsmThreads, 0, c.stream>>>(a);
+        c.launches += 1;
         LF_CUDA(cudaGetLastError());
     }
 }

@@ -1,0 +1,784 @@
+// Preconditioned CG as a device-driven CUDA graph.
+//
+// Same recurrences as the persistent kernel in pcg.cu (pcg_solve,
+// src/solver.cpp:532-627, in FP64; the FP32-inner / FP64-refinement scheme in
+// mixed precision), but every phase is its own kernel at full occupancy and the
+// loop runs inside one CUDA graph without host round trips:
+//
+//   init -> WHILE(loop) { product ; update ; [FP64: p update]
+//                         [mixed: IF(refine) { FP64 residual ; re-precondition }] }
+//
+// The WHILE and IF bodies are graph conditional nodes; their conditions are set
+// from the device (cudaGraphSetConditional) by the block that finishes each
+// reduction.  Scalars (rho, alpha, beta, norms, counters) live in a device
+// CgState.  Dot products are reduced deterministically: every block publishes
+// its partial, and the last block to arrive adds them in block order.
+//
+// Products: a quarter warp per CSR row; for FP64 BSR each 2x2 block is read as
+// two 16-byte halves by a lane pair, so a warp reads 512 contiguous bytes; for
+// FP32 BSR a quarter warp reads one 16-byte block per lane.  Matrix loads carry
+// the evict-first hint so the vectors stay in L2.
+#include "common.cuh"
+#include "kernels.hpp"
+
+#include <cmath>
+
+namespace lfgpu {
+namespace {
+
+constexpr int kThreads = 256;
+
+struct CgState {
+    double rho, alpha, beta, r0, rnorm, rmax, rtrue, rtrue_prev;
+    long long it, refs;
+    int status, converged, stagnated, done, no_progress, refine;
+    unsigned int count[4];
+};
+
+struct CgArgs {
+    int n, nb;
+    const int* rowptr;
+    const int* col;
+    const double* K;
+    const float* K32;
+    const int* brow;
+    const int* bcol;
+    const double2* bval64;
+    const float4* bval32;
+    const float* dhi;
+    const float* dlo;
+    const double* invd64;
+    const double* blk64;
+    const float* invd32;
+    const float* blk32;
+    const double* f;
+    const double* x0;
+    double* x;
+    double* r;
+    double* z;
+    double* p;
+    double* q;
+    double* r64;
+    float* r32;
+    float* z32;
+    float* pa;
+    float* pb;
+    float* q32;
+    double* partials;  // 4 slots x blocks x 4
+    int blocks;
+    CgState* st;
+    DeviceStatus* status;
+    double target, reduction;
+    long long maxit, max_ref;
+    int restart;
+    cudaGraphConditionalHandle loop, branch;
+};
+
+__device__ __forceinline__ void set_loop(const CgArgs& a, bool go) { cudaGraphSetConditional(a.loop, go ? 1u : 0u); }
+
+// Block sums of K values, then the last block to finish adds every block's sums in
+// block order and runs fin(totals) on thread 0.
+template <int K, typename Final>
+__device__ __forceinline__ void reduce_last(const CgArgs& a, int slot, double (&v)[K], Final&& fin) {
+    __shared__ double s_red[32 * kMaxReduce];
+    __shared__ int s_last;
+    block_sum<K>(v, s_red);
+    double* part = a.partials + static_cast<size_t>(slot) * a.blocks * kMaxReduce;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) part[blockIdx.x * kMaxReduce + k] = v[k];
+        __threadfence();
+        const unsigned t = atomicAdd(&a.st->count[slot], 1u);
+        s_last = t == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+    for (int b = threadIdx.x; b < static_cast<int>(gridDim.x); b += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[k] += __ldcg(part + b * kMaxReduce + k);
+    }
+    block_sum<K>(acc, s_red);
+    if (threadIdx.x == 0) {
+        a.st->count[slot] = 0;
+        fin(acc);
+    }
+}
+
+// Warp-uniform loop over row groups of 8 (quarter warp per row) across the grid.
+template <typename F>
+__device__ __forceinline__ void rows_by_quad(int rows, F&& f) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int base = warp * 8; base < rows; base += nwarps * 8) {
+        const int row = base + (lane >> 2);
+        f(row < rows, row, lane & 3);
+    }
+}
+
+__device__ __forceinline__ double quad_sum(double v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    return v + __shfl_xor_sync(0xffffffffu, v, 2);
+}
+__device__ __forceinline__ float quad_sum(float v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    return v + __shfl_xor_sync(0xffffffffu, v, 2);
+}
+
+// y = K x in FP64 for CSR rows; out(row, y) on the quad leader.
+template <typename G, typename Out>
+__device__ __forceinline__ void csr64_rows(const CgArgs& a, const G& g, Out&& out) {
+    rows_by_quad(a.n, [&](bool act, int row, int sub) {
+        double s = 0.0;
+        if (act) {
+            const int b = __ldg(a.rowptr + row), e = __ldg(a.rowptr + row + 1);
+            for (int k = b + sub; k < e; k += 8) {  // two independent units in flight per lane
+                const bool two = k + 4 < e;
+                const int c0 = ld_stream(a.col + k), c1 = two ? ld_stream(a.col + k + 4) : c0;
+                const double v0 = ld_stream(a.K + k), v1 = two ? ld_stream(a.K + k + 4) : 0.0;
+                const double x0 = g(c0), x1 = g(c1);
+                s += v0 * x0;
+                s += v1 * x1;
+            }
+        }
+        s = quad_sum(s);
+        if (act && sub == 0) out(row, s);
+    });
+}
+
+// y = K x in FP64 for BSR block rows: lane pairs read the two 16-byte halves of a
+// block; even lanes sum the top row, odd lanes the bottom row.
+template <typename G, typename Out>
+__device__ __forceinline__ void bsr64_rows(const CgArgs& a, const G& g, Out&& out) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int l8 = lane & 7, half = l8 & 1, pair = l8 >> 1;
+    for (int base = warp * 4; base < a.nb; base += nwarps * 4) {
+        const int node = base + (lane >> 3);
+        double s = 0.0;
+        if (node < a.nb) {
+            const int b = __ldg(a.brow + node), e = __ldg(a.brow + node + 1);
+            for (int k = b + pair; k < e; k += 8) {  // two blocks in flight per lane
+                const bool two = k + 4 < e;
+                const double2 v0 = ld_stream(a.bval64 + 2 * static_cast<size_t>(k) + half);
+                const double2 v1 = two ? ld_stream(a.bval64 + 2 * static_cast<size_t>(k + 4) + half)
+                                       : make_double2(0.0, 0.0);
+                const int c0 = ld_stream(a.bcol + k), c1 = two ? ld_stream(a.bcol + k + 4) : c0;
+                const double2 x0 = g(c0), x1 = g(c1);
+                s += v0.x * x0.x + v0.y * x0.y;
+                s += v1.x * x1.x + v1.y * x1.y;
+            }
+        }
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        s += __shfl_xor_sync(0xffffffffu, s, 4);
+        const double s1 = __shfl_down_sync(0xffffffffu, s, 1);
+        if (node < a.nb && l8 == 0) out(node, make_double2(s, s1));
+    }
+}
+
+// FP32 BSR block rows, quarter warp per block row (one 16-byte block per lane).
+template <typename G, typename Out>
+__device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& out) {
+    rows_by_quad(a.nb, [&](bool act, int node, int sub) {
+        float s0 = 0.f, s1 = 0.f;
+        if (act) {
+            const int b = __ldg(a.brow + node), e = __ldg(a.brow + node + 1);
+            for (int k = b + sub; k < e; k += 8) {  // two blocks in flight per lane
+                const bool two = k + 4 < e;
+                const float4 v0 = ld_stream(a.bval32 + k);
+                const float4 v1 = two ? ld_stream(a.bval32 + k + 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+                const int c0 = ld_stream(a.bcol + k), c1 = two ? ld_stream(a.bcol + k + 4) : c0;
+                const float2 x0 = g(c0), x1 = g(c1);
+                s0 += v0.x * x0.x + v0.y * x0.y;
+                s1 += v0.z * x0.x + v0.w * x0.y;
+                s0 += v1.x * x1.x + v1.y * x1.y;
+                s1 += v1.z * x1.x + v1.w * x1.y;
+            }
+        }
+        s0 = quad_sum(s0);
+        s1 = quad_sum(s1);
+        if (act && sub == 0) out(node, make_float2(s0, s1));
+    });
+}
+
+template <typename G, typename Out>
+__device__ __forceinline__ void csr32_rows(const CgArgs& a, const G& g, Out&& out) {
+    rows_by_quad(a.n, [&](bool act, int row, int sub) {
+        float s = 0.f;
+        if (act) {
+            const int b = __ldg(a.rowptr + row), e = __ldg(a.rowptr + row + 1);
+            for (int k = b + sub; k < e; k += 8) {  // two independent units in flight per lane
+                const bool two = k + 4 < e;
+                const int c0 = ld_stream(a.col + k), c1 = two ? ld_stream(a.col + k + 4) : c0;
+                const float v0 = ld_stream(a.K32 + k), v1 = two ? ld_stream(a.K32 + k + 4) : 0.f;
+                const float x0 = g(c0), x1 = g(c1);
+                s += v0 * x0;
+                s += v1 * x1;
+            }
+        }
+        s = quad_sum(s);
+        if (act && sub == 0) out(row, s);
+    });
+}
+
+__device__ __forceinline__ double2 block2_apply(const double* __restrict__ blk, int i, double r0, double r1) {
+    const double f0 = blk[3 * i], f1 = blk[3 * i + 1], f2 = blk[3 * i + 2];
+    double s0 = __dmul_rn(r0, f0);
+    double s1 = __dmul_rn(__dsub_rn(r1, __dmul_rn(f1, s0)), f2);
+    s1 = __dmul_rn(s1, f2);
+    s0 = __dmul_rn(__dsub_rn(s0, __dmul_rn(f1, s1)), f0);
+    return make_double2(s0, s1);
+}
+
+__device__ __forceinline__ float2 block2_apply32(const float* __restrict__ blk, int i, float r0, float r1) {
+    const float f0 = blk[3 * i], f1 = blk[3 * i + 1], f2 = blk[3 * i + 2];
+    float s0 = r0 * f0;
+    float s1 = (r1 - f1 * s0) * f2;
+    s1 = s1 * f2;
+    s0 = (s0 - f1 * s1) * f0;
+    return make_float2(s0, s1);
+}
+
+template <int PRECOND>
+__device__ __forceinline__ double2 precond64(const CgArgs& a, int i, double2 rv) {
+    if (PRECOND == LFGPU_PRECOND_JACOBI) {
+        const double2 d = reinterpret_cast<const double2*>(a.invd64)[i];
+        return make_double2(d.x * rv.x, d.y * rv.y);
+    }
+    return block2_apply(a.blk64, i, rv.x, rv.y);
+}
+
+template <int PRECOND>
+__device__ __forceinline__ float2 precond32(const CgArgs& a, int i, float2 rv) {
+    if (PRECOND == LFGPU_PRECOND_JACOBI) {
+        const float2 d = reinterpret_cast<const float2*>(a.invd32)[i];
+        return make_float2(d.x * rv.x, d.y * rv.y);
+    }
+    return block2_apply32(a.blk32, i, rv.x, rv.y);
+}
+
+#define GRID_NODES(i) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nb; i += gridDim.x * blockDim.x)
+
+// ------------------------------------------------------------------ FP64 kernels
+// r = f - K x0 for a warm start.
+template <int STORAGE>
+__global__ void __launch_bounds__(kThreads) cg64_residual(CgArgs a) {
+    if (STORAGE == LFGPU_STORAGE_CSR) {
+        csr64_rows(a, [&](int c) { return a.x0[c]; }, [&](int row, double y) { a.r[row] = a.f[row] - y; });
+    } else {
+        const double2* x02 = reinterpret_cast<const double2*>(a.x0);
+        bsr64_rows(a, [&](int c) { return x02[c]; }, [&](int node, double2 y) {
+            a.r[2 * node] = a.f[2 * node] - y.x;
+            a.r[2 * node + 1] = a.f[2 * node + 1] - y.y;
+        });
+    }
+}
+
+template <int PRECOND>
+__global__ void __launch_bounds__(kThreads) cg64_init(CgArgs a) {
+    double v[2] = {0.0, 0.0};
+    double2* x2 = reinterpret_cast<double2*>(a.x);
+    double2* r2 = reinterpret_cast<double2*>(a.r);
+    double2* z2 = reinterpret_cast<double2*>(a.z);
+    double2* p2 = reinterpret_cast<double2*>(a.p);
+    const double2* f2 = reinterpret_cast<const double2*>(a.f);
+    GRID_NODES(i) {
+        const double2 rv = a.x0 ? r2[i] : f2[i];
+        const double2 zv = precond64<PRECOND>(a, i, rv);
+        r2[i] = rv;
+        z2[i] = zv;
+        p2[i] = zv;
+        x2[i] = a.x0 ? reinterpret_cast<const double2*>(a.x0)[i] : make_double2(0.0, 0.0);
+        v[0] += rv.x * rv.x + rv.y * rv.y;
+        v[1] += rv.x * zv.x + rv.y * zv.y;
+    }
+    reduce_last<2>(a, 0, v, [&](const double* t) {
+        CgState* s = a.st;
+        s->r0 = s->rnorm = sqrt(fmax(0.0, t[0]));
+        s->rho = t[1];
+        s->it = 0;
+        if (s->r0 <= a.target) {
+            s->converged = 1;
+            s->done = 1;
+        } else if (!(t[1] > 0.0) || !isfinite(t[1])) {
+            s->status = LFGPU_ERR_RHO_INITIAL;
+            s->done = 1;
+        }
+        set_loop(a, !s->done);
+    });
+}
+
+template <int STORAGE>
+__global__ void __launch_bounds__(kThreads) cg64_product(CgArgs a) {
+    if (a.st->done) return;
+    double v[1] = {0.0};
+    if (STORAGE == LFGPU_STORAGE_CSR) {
+        csr64_rows(a, [&](int c) { return a.p[c]; }, [&](int row, double y) {
+            a.q[row] = y;
+            v[0] += a.p[row] * y;
+        });
+    } else {
+        const double2* p2 = reinterpret_cast<const double2*>(a.p);
+        bsr64_rows(a, [&](int c) { return p2[c]; }, [&](int node, double2 y) {
+            reinterpret_cast<double2*>(a.q)[node] = y;
+            const double2 pv = p2[node];
+            v[0] += pv.x * y.x + pv.y * y.y;
+        });
+    }
+    reduce_last<1>(a, 1, v, [&](const double* t) {
+        CgState* s = a.st;
+        if (!(t[0] > 0.0) || !isfinite(t[0])) {
+            s->status = LFGPU_ERR_NOT_SPD;
+            s->done = 1;
+            set_loop(a, false);
+        } else {
+            s->alpha = s->rho / t[0];
+        }
+    });
+}
+
+template <int PRECOND>
+__global__ void __launch_bounds__(kThreads) cg64_update(CgArgs a) {
+    if (a.st->done) return;
+    const double alpha = a.st->alpha;
+    double v[2] = {0.0, 0.0};
+    double2* x2 = reinterpret_cast<double2*>(a.x);
+    double2* r2 = reinterpret_cast<double2*>(a.r);
+    double2* z2 = reinterpret_cast<double2*>(a.z);
+    const double2* p2 = reinterpret_cast<const double2*>(a.p);
+    const double2* q2 = reinterpret_cast<const double2*>(a.q);
+    GRID_NODES(i) {
+        const double2 pv = p2[i], qv = q2[i];
+        double2 xv = x2[i], rv = r2[i];
+        xv.x += alpha * pv.x;
+        xv.y += alpha * pv.y;
+        rv.x -= alpha * qv.x;
+        rv.y -= alpha * qv.y;
+        const double2 zv = precond64<PRECOND>(a, i, rv);
+        x2[i] = xv;
+        r2[i] = rv;
+        z2[i] = zv;
+        v[0] += rv.x * rv.x + rv.y * rv.y;
+        v[1] += rv.x * zv.x + rv.y * zv.y;
+    }
+    reduce_last<2>(a, 2, v, [&](const double* t) {
+        CgState* s = a.st;
+        s->it += 1;
+        s->rnorm = sqrt(fmax(0.0, t[0]));
+        if (s->rnorm <= a.target) {
+            s->converged = 1;
+            s->done = 1;
+        } else if (!(t[1] > 0.0) || !isfinite(t[1])) {
+            s->status = LFGPU_ERR_RHO;
+            s->done = 1;
+        } else {
+            s->beta = t[1] / s->rho;
+            s->rho = t[1];
+            if (s->it >= a.maxit) s->done = 1;
+        }
+        set_loop(a, !s->done);
+    });
+}
+
+__global__ void __launch_bounds__(kThreads) cg64_direction(CgArgs a) {
+    if (a.st->done) return;
+    const double beta = a.st->beta;
+    double2* p2 = reinterpret_cast<double2*>(a.p);
+    const double2* z2 = reinterpret_cast<const double2*>(a.z);
+    GRID_NODES(i) {
+        const double2 zv = z2[i];
+        double2 pv = p2[i];
+        pv.x = zv.x + beta * pv.x;
+        pv.y = zv.y + beta * pv.y;
+        p2[i] = pv;
+    }
+}
+
+// ------------------------------------------------------------------ mixed kernels
+__device__ __forceinline__ float pnew(float z, float p, float beta) { return __fmaf_rn(beta, p, z); }
+__device__ __forceinline__ float with_diag(float off, float hi, float lo, float x) { return fmaf(hi, x, off) + lo * x; }
+
+template <int PRECOND>
+__global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
+    double v[2] = {0.0, 0.0};
+    const double2* f2 = reinterpret_cast<const double2*>(a.f);
+    GRID_NODES(i) {
+        const double2 fv = f2[i];
+        const float2 rv = make_float2(static_cast<float>(fv.x), static_cast<float>(fv.y));
+        const float2 zv = precond32<PRECOND>(a, i, rv);
+        reinterpret_cast<double2*>(a.x)[i] = make_double2(0.0, 0.0);
+        reinterpret_cast<double2*>(a.r64)[i] = fv;
+        reinterpret_cast<float2*>(a.r32)[i] = rv;
+        reinterpret_cast<float2*>(a.z32)[i] = zv;
+        reinterpret_cast<float2*>(a.pa)[i] = make_float2(0.f, 0.f);
+        reinterpret_cast<float2*>(a.pb)[i] = make_float2(0.f, 0.f);
+        v[0] += fv.x * fv.x + fv.y * fv.y;
+        v[1] += static_cast<double>(rv.x * zv.x + rv.y * zv.y);
+    }
+    reduce_last<2>(a, 0, v, [&](const double* t) {
+        CgState* s = a.st;
+        s->r0 = s->rnorm = s->rmax = s->rtrue = s->rtrue_prev = sqrt(fmax(0.0, t[0]));
+        s->rho = t[1];
+        s->beta = 0.0;
+        s->it = 0;
+        s->refs = 0;
+        if (s->r0 <= a.target) {
+            s->converged = 1;
+            s->done = 1;
+        } else if (!(t[1] > 0.0) || !isfinite(t[1])) {
+            s->status = LFGPU_ERR_RHO_INITIAL;
+            s->done = 1;
+        }
+        set_loop(a, !s->done);
+    });
+}
+
+// q = K32 p with p = z + beta p_old formed on the fly; each row writes its p.
+template <int STORAGE>
+__global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
+    if (a.st->done) return;
+    const float beta = static_cast<float>(a.st->beta);
+    const bool odd = a.st->it & 1;
+    const float* po = odd ? a.pb : a.pa;
+    float* pc = odd ? a.pa : a.pb;
+    float acc = 0.f;
+    if (STORAGE == LFGPU_STORAGE_CSR) {
+        const float* z = a.z32;
+        csr32_rows(a, [&](int c) { return pnew(z[c], po[c], beta); }, [&](int row, float off) {
+            const float pn = pnew(z[row], po[row], beta);
+            const float y = with_diag(off, a.dhi[row], a.dlo[row], pn);
+            pc[row] = pn;
+            a.q32[row] = y;
+            acc += pn * y;
+        });
+    } else {
+        const float2* z2 = reinterpret_cast<const float2*>(a.z32);
+        const float2* po2 = reinterpret_cast<const float2*>(po);
+        const float2* hi2 = reinterpret_cast<const float2*>(a.dhi);
+        const float2* lo2 = reinterpret_cast<const float2*>(a.dlo);
+        bsr32_rows(a,
+                   [&](int c) {
+                       const float2 zv = z2[c], pv = po2[c];
+                       return make_float2(pnew(zv.x, pv.x, beta), pnew(zv.y, pv.y, beta));
+                   },
+                   [&](int node, float2 off) {
+                       const float2 zv = z2[node], pv = po2[node];
+                       const float2 pn = make_float2(pnew(zv.x, pv.x, beta), pnew(zv.y, pv.y, beta));
+                       const float2 h = hi2[node], l = lo2[node];
+                       const float2 y = make_float2(with_diag(off.x, h.x, l.x, pn.x), with_diag(off.y, h.y, l.y, pn.y));
+                       reinterpret_cast<float2*>(pc)[node] = pn;
+                       reinterpret_cast<float2*>(a.q32)[node] = y;
+                       acc += pn.x * y.x + pn.y * y.y;
+                   });
+    }
+    double v[1] = {acc};
+    reduce_last<1>(a, 1, v, [&](const double* t) {
+        CgState* s = a.st;
+        if (!(t[0] > 0.0) || !isfinite(t[0])) {
+            s->status = LFGPU_ERR_NOT_SPD;
+            s->done = 1;
+            set_loop(a, false);
+        } else {
+            s->alpha = s->rho / t[0];
+        }
+    });
+}
+
+template <int PRECOND>
+__global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
+    if (a.st->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.branch, 0u);
+        return;
+    }
+    const double alpha64 = a.st->alpha;
+    const float alpha = static_cast<float>(alpha64);
+    const bool odd = a.st->it & 1;
+    const float2* pc2 = reinterpret_cast<const float2*>(odd ? a.pa : a.pb);
+    const float2* q2 = reinterpret_cast<const float2*>(a.q32);
+    float2* r2 = reinterpret_cast<float2*>(a.r32);
+    float2* z2 = reinterpret_cast<float2*>(a.z32);
+    double2* x2 = reinterpret_cast<double2*>(a.x);
+    float rr = 0.f, rz = 0.f;
+    GRID_NODES(i) {
+        const float2 pv = pc2[i], qv = q2[i];
+        double2 xv = x2[i];
+        float2 rv = r2[i];
+        xv.x += alpha64 * static_cast<double>(pv.x);
+        xv.y += alpha64 * static_cast<double>(pv.y);
+        rv.x -= alpha * qv.x;
+        rv.y -= alpha * qv.y;
+        const float2 zv = precond32<PRECOND>(a, i, rv);
+        x2[i] = xv;
+        r2[i] = rv;
+        z2[i] = zv;
+        rr += rv.x * rv.x + rv.y * rv.y;
+        rz += rv.x * zv.x + rv.y * zv.y;
+    }
+    double v[2] = {rr, rz};
+    reduce_last<2>(a, 2, v, [&](const double* t) {
+        CgState* s = a.st;
+        s->it += 1;
+        const double rn = sqrt(fmax(0.0, t[0]));
+        s->rnorm = rn;
+        s->rmax = fmax(s->rmax, rn);
+        const bool refine = rn <= a.reduction * s->rmax || rn <= a.target || s->it >= a.maxit;
+        s->refine = refine;
+        if (!refine) {
+            if (!(t[1] > 0.0) || !isfinite(t[1])) {
+                s->status = LFGPU_ERR_RHO;
+                s->done = 1;
+            } else {
+                s->beta = t[1] / s->rho;
+                s->rho = t[1];
+            }
+        }
+        cudaGraphSetConditional(a.branch, refine && !s->done ? 1u : 0u);
+        set_loop(a, !s->done);
+    });
+}
+
+// FP64 residual replacement: r64 = f - K64 x, r32 = r64.
+template <int STORAGE>
+__global__ void __launch_bounds__(kThreads) mx_residual(CgArgs a) {
+    double v[1] = {0.0};
+    if (STORAGE == LFGPU_STORAGE_CSR) {
+        csr64_rows(a, [&](int c) { return a.x[c]; }, [&](int row, double y) {
+            const double rv = a.f[row] - y;
+            a.r64[row] = rv;
+            a.r32[row] = static_cast<float>(rv);
+            v[0] += rv * rv;
+        });
+    } else {
+        const double2* x2 = reinterpret_cast<const double2*>(a.x);
+        bsr64_rows(a, [&](int c) { return x2[c]; }, [&](int node, double2 y) {
+            const double2 fv = reinterpret_cast<const double2*>(a.f)[node];
+            const double2 rv = make_double2(fv.x - y.x, fv.y - y.y);
+            reinterpret_cast<double2*>(a.r64)[node] = rv;
+            reinterpret_cast<float2*>(a.r32)[node] = make_float2(static_cast<float>(rv.x), static_cast<float>(rv.y));
+            v[0] += rv.x * rv.x + rv.y * rv.y;
+        });
+    }
+    reduce_last<1>(a, 3, v, [&](const double* t) {
+        CgState* s = a.st;
+        s->refs += 1;
+        const double rt = sqrt(fmax(0.0, t[0]));
+        s->rtrue = rt;
+        if (rt <= a.target) {
+            s->converged = 1;
+            s->done = 1;
+        } else if (s->refs >= a.max_ref || s->it >= a.maxit) {
+            s->done = 1;
+        } else {
+            s->no_progress = rt >= s->rtrue_prev ? s->no_progress + 1 : 0;
+            if (s->no_progress >= 3) {
+                s->stagnated = 1;
+                s->done = 1;
+            }
+            s->rtrue_prev = fmin(s->rtrue_prev, rt);
+            s->rmax = rt;
+        }
+        set_loop(a, !s->done);
+    });
+}
+
+template <int PRECOND>
+__global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
+    if (a.st->done) return;
+    const float2* r2 = reinterpret_cast<const float2*>(a.r32);
+    float2* z2 = reinterpret_cast<float2*>(a.z32);
+    float rz = 0.f;
+    GRID_NODES(i) {
+        const float2 rv = r2[i];
+        const float2 zv = precond32<PRECOND>(a, i, rv);
+        z2[i] = zv;
+        rz += rv.x * zv.x + rv.y * zv.y;
+    }
+    double v[1] = {rz};
+    reduce_last<1>(a, 2, v, [&](const double* t) {
+        CgState* s = a.st;
+        if (!(t[0] > 0.0) || !isfinite(t[0])) {
+            s->status = LFGPU_ERR_RHO;
+            s->done = 1;
+        } else {
+            s->beta = a.restart ? 0.0 : t[0] / s->rho;
+            s->rho = t[0];
+        }
+        set_loop(a, !s->done);
+    });
+}
+
+// ------------------------------------------------------------------ graph assembly
+struct GraphBuilder {
+    Context& c;
+    cudaGraph_t graph = nullptr;
+    ~GraphBuilder() {
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
+template <typename K>
+void add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep, int ndep, K kernel, int blocks,
+                CgArgs* args) {
+    cudaKernelNodeParams p = {};
+    p.func = reinterpret_cast<void*>(kernel);
+    p.gridDim = dim3(blocks);
+    p.blockDim = dim3(kThreads);
+    p.sharedMemBytes = 0;
+    void* params[1] = {args};
+    p.kernelParams = params;
+    LF_CUDA(cudaGraphAddKernelNode(node, g, dep, ndep, &p));
+}
+
+cudaGraphNode_t add_conditional(cudaGraph_t g, const cudaGraphNode_t* dep, int ndep, cudaGraphConditionalHandle h,
+                                cudaGraphConditionalNodeType type, cudaGraph_t* body) {
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = type;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    LF_CUDA(cudaGraphAddNode(&node, g, dep, nullptr, ndep, &np));
+    *body = np.conditional.phGraph_out[0];
+    return node;
+}
+
+template <int STORAGE, int PRECOND>
+void build_fp64(cudaGraph_t g, CgArgs* a, int blocks) {
+    cudaGraphNode_t n_res = nullptr, n_init, n_loop;
+    if (a->x0) add_kernel(g, &n_res, nullptr, 0, cg64_residual<STORAGE>, blocks, a);
+    add_kernel(g, &n_init, a->x0 ? &n_res : nullptr, a->x0 ? 1 : 0, cg64_init<PRECOND>, blocks, a);
+    cudaGraph_t body;
+    n_loop = add_conditional(g, &n_init, 1, a->loop, cudaGraphCondTypeWhile, &body);
+    (void)n_loop;
+    cudaGraphNode_t k1, k2, k3;
+    add_kernel(body, &k1, nullptr, 0, cg64_product<STORAGE>, blocks, a);
+    add_kernel(body, &k2, &k1, 1, cg64_update<PRECOND>, blocks, a);
+    add_kernel(body, &k3, &k2, 1, cg64_direction, blocks, a);
+}
+
+template <int STORAGE, int PRECOND>
+void build_mixed(cudaGraph_t g, CgArgs* a, int blocks) {
+    cudaGraphNode_t n_init;
+    add_kernel(g, &n_init, nullptr, 0, mx_init<PRECOND>, blocks, a);
+    cudaGraph_t body;
+    add_conditional(g, &n_init, 1, a->loop, cudaGraphCondTypeWhile, &body);
+    // The IF node lives in the loop body, so its handle belongs to that graph.
+    LF_CUDA(cudaGraphConditionalHandleCreate(&a->branch, body, 0, 0));
+    cudaGraphNode_t k1, k2, k3, k4;
+    add_kernel(body, &k1, nullptr, 0, mx_product<STORAGE>, blocks, a);
+    add_kernel(body, &k2, &k1, 1, mx_update<PRECOND>, blocks, a);
+    cudaGraph_t branch;
+    add_conditional(body, &k2, 1, a->branch, cudaGraphCondTypeIf, &branch);
+    add_kernel(branch, &k3, nullptr, 0, mx_residual<STORAGE>, blocks, a);
+    add_kernel(branch, &k4, &k3, 1, mx_reprecondition<PRECOND>, blocks, a);
+}
+
+}  // namespace
+
+PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
+    const i64 n = c.n;
+    LF_REQUIRE(n % 2 == 0, LFGPU_ERR_ARGUMENT, "the GPU PCG needs an even number of DOFs (u,v pairs)");
+    const int blocks = c.num_sms * (2048 / kThreads);
+    CgArgs a{};
+    a.n = static_cast<int>(n);
+    a.nb = static_cast<int>(n / 2);
+    a.rowptr = c.rowptr;
+    a.col = c.col;
+    a.K = c.K;
+    a.invd64 = c.inv_diag64;
+    a.blk64 = c.blk64;
+    a.invd32 = c.inv_diag32;
+    a.blk32 = c.blk32;
+    a.f = s.rhs;
+    a.x0 = s.x0;
+    a.x = s.x;
+    for (auto& b : c.v64) b.ensure(n);
+    a.r = c.v64[0];
+    a.z = c.v64[1];
+    a.p = c.v64[2];
+    a.q = c.v64[3];
+    a.r64 = c.v64[4];
+    if (s.storage == LFGPU_STORAGE_BSR) {
+        ensure_bsr(c);
+        a.brow = c.brow;
+        a.bcol = c.bcol;
+        a.bval64 = reinterpret_cast<const double2*>(c.bval64.p);
+    }
+    if (s.mixed) {
+        for (auto& b : c.v32) b.ensure(n);
+        a.r32 = c.v32[0];
+        a.z32 = c.v32[1];
+        a.pa = c.v32[2];
+        a.pb = c.v32[3];
+        a.q32 = c.v32[4];
+        if (s.storage == LFGPU_STORAGE_BSR) {
+            ensure_bsr32(c);
+            a.bval32 = reinterpret_cast<const float4*>(c.bval32.p);
+        } else {
+            ensure_csr32(c);
+            a.K32 = c.K32;
+        }
+        a.dhi = c.diag_hi;
+        a.dlo = c.diag_lo;
+    }
+    c.partials.ensure(static_cast<size_t>(kSlots) * kMaxReduce * blocks);
+    a.partials = c.partials;
+    a.blocks = blocks;
+    c.cg_state.ensure(sizeof(CgState));
+    a.st = reinterpret_cast<CgState*>(c.cg_state.p);
+    a.status = c.status;
+    a.target = s.tolerance;
+    a.reduction = s.inner_reduction;
+    a.maxit = s.max_iterations;
+    a.max_ref = s.max_refinements;
+    a.restart = s.restart;
+    LF_CUDA(cudaMemsetAsync(c.cg_state.p, 0, sizeof(CgState), c.stream));
+
+    GraphBuilder gb{c};
+    LF_CUDA(cudaGraphCreate(&gb.graph, 0));
+    LF_CUDA(cudaGraphConditionalHandleCreate(&a.loop, gb.graph, 0, 0));
+    const bool csr = s.storage == LFGPU_STORAGE_CSR;
+    const bool jac = s.precond == LFGPU_PRECOND_JACOBI;
+    if (!s.mixed) {
+        if (csr && jac) build_fp64<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
+        else if (csr) build_fp64<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
+        else if (jac) build_fp64<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
+        else build_fp64<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
+    } else {
+        if (csr && jac) build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
+        else if (csr) build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
+        else if (jac) build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
+        else build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
+    }
+    cudaGraphExec_t exec = nullptr;
+    LF_CUDA(cudaGraphInstantiate(&exec, gb.graph, 0));
+    cudaError_t err = cudaEventRecord(c.ev_a, c.stream);
+    if (err == cudaSuccess) err = cudaGraphLaunch(exec, c.stream);
+    if (err == cudaSuccess) err = cudaEventRecord(c.ev_b, c.stream);
+    cudaGraphExecDestroy(exec);
+    LF_CUDA(err);
+    *kernel_ms = elapsed_ms(c);
+    CgState st{};
+    LF_CUDA(cudaMemcpyAsync(&st, c.cg_state.p, sizeof(st), cudaMemcpyDeviceToHost, c.stream));
+    check_status(c);
+    // Kernel nodes that ran: residual (warm start) + init, then per loop pass the
+    // body (FP64: product, update, direction; mixed: product, update) and per
+    // residual replacement the two branch kernels.
+    c.launches += (s.x0 ? 1 : 0) + 1 + (s.mixed ? 2 * st.it + 2 * st.refs : 3 * st.it);
+    PcgResult r{};
+    r.iterations = st.it;
+    r.refinements = st.refs;
+    r.initial_residual = st.r0;
+    r.final_residual = s.mixed ? st.rtrue : st.rnorm;
+    r.status = st.status;
+    r.converged = st.converged;
+    r.stagnated = st.stagnated;
+    return r;
+}
+
+}  // namespace lfgpu

@@ -75,6 +75,7 @@ struct PcgResult {
     int converged;
     int stagnated;
     int pad;
+    unsigned long long phase_ns[6];  // CTA 0's time per phase, summed over iterations
 };
 
 // Scalars of the grid-wide reductions: one slot per barrier of an iteration,
@@ -152,8 +153,26 @@ struct Context {
     Buf<unsigned long long> bar;          // grid barrier counter
     Buf<DeviceStatus> status;
     Buf<PcgResult> pcg_result;
+    Buf<char> cg_state;
     Buf<double> scratch64;
     bool solved = false;
+
+    // FP32 inner matrices keep their diagonal as an FP32 (hi, lo) pair that also
+    // absorbs each row's off-diagonal rounding error (built with K32 / bval32).
+    Buf<float> diag_hi, diag_lo;
+
+    // Tile schedules of the persistent product phase: per matrix format, the row
+    // ranges each CTA streams through shared memory (see pcg.cu).
+    struct Schedule {
+        Buf<int2> tiles;
+        Buf<int> cta;
+        int grid = 0;
+        int units = 0;
+        unsigned long long version = ~0ull;
+    };
+    Schedule sched[4];
+    unsigned long long pattern_version = 0;
+    std::vector<int> h_brow;
 
     // ic0 state (built per K version)
     unsigned long long ic0_version = ~0ull;
@@ -164,6 +183,8 @@ struct Context {
     i64 ic0_breakdowns = 0;
 
     lfgpu_timings timings{};
+    i64 launches = 0;                 // kernels launched by this handle (graph nodes included)
+    cudaEvent_t user_ev[8] = {};      // lfgpu_event_record slots
 };
 
 void check_status(Context& c);   // syncs the stream, raises the first device failure
@@ -290,6 +311,66 @@ __device__ __forceinline__ bool grid_sum(double (&v)[K], double* partials, int s
 #pragma unroll
     for (int k = 0; k < K; ++k) v[k] = s_red[k];
     __syncthreads();
+    return true;
+}
+
+// ------------------------------------------------------------------ bulk async copies
+// cp.async.bulk (1-D TMA) into shared memory, completion tracked by an mbarrier.
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long l2_evict_first_policy() {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// Global -> shared bulk copy; dst, src and bytes must be multiples of 16.
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned bytes, unsigned long long* bar,
+                                          unsigned long long policy) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+
+// Order this CTA's earlier generic-proxy shared-memory accesses before later bulk copies.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for an mbarrier phase, bounded in time; records LFGPU_ERR_TIMEOUT on expiry.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, DeviceStatus* status,
+                                          unsigned long long limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long start = global_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (global_ns() - start > limit_ns) {
+            atomicExch(&status->abort, 1u);
+            record_failure(status, LFGPU_ERR_TIMEOUT, static_cast<int>(blockIdx.x));
+            return false;
+        }
+    }
     return true;
 }
 

@@ -39,6 +39,9 @@ struct SolveSetup {
 };
 PcgResult run_pcg(Context& c, const SolveSetup& s, float* kernel_ms);
 
+// cg_graph.cu: the same solver as a device-driven CUDA graph of per-phase kernels
+PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms);
+
 // ic0.cu
 void ensure_ic0(Context& c, bool fp32);
 PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double* apply_ms);

