@@ -305,11 +305,17 @@ def run_ours(args) -> int:
         # --profile-iters iterations, then three standalone products of each kind.
         capped = ctx.options(tol, args.profile_iters, args.storage, args.precond, "mixed", "reliable")
         ms, rep = step(capped)
+        unrolled = ctx.options(tol, 10 ** 6, args.storage, args.precond, "mixed", "reliable",
+                               unrolled=args.profile_iters)
+        ms_u, rep_u = step(unrolled)
         x = np.random.default_rng(0).standard_normal(n)
         for st in ("csr", "bsr"):
             for prec in ("fp64", "mixed"):
                 ctx.spmv(x, 1, st, prec, repeat=3)
-        print(json.dumps({"profile_iters": args.profile_iters, "step_ms": ms, "iterations": rep.iterations}))
+        print(json.dumps({"profile_iters": args.profile_iters, "conditional_step_ms": ms,
+                          "conditional_solve_ms": rep.solve_ms, "iterations": rep.iterations,
+                          "unrolled_step_ms": ms_u, "unrolled_solve_ms": rep_u.solve_ms,
+                          "unrolled_iterations": rep_u.iterations}))
         ctx.close()
         return 0
     for _ in range(args.warmup):

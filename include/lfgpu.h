@@ -91,7 +91,9 @@ typedef struct lfgpu_solve_options {
     int64_t max_refinements;   /* mixed: cap on FP64 residual replacements */
     int32_t persistent;        /* 1: one persistent cooperative kernel; 0: device-driven CUDA graph of
                                   per-phase kernels (conditional WHILE node) */
-    int32_t reserved;
+    int32_t unrolled;          /* profiling only, graph loop: > 0 replaces the conditional loop by a plain
+                                  graph of this many iterations (profilers do not descend into
+                                  conditional bodies); the solve stops there */
 } lfgpu_solve_options;
 
 /* Mirrors LinearSolverReport (include/lightfem/solver.hpp:12-34) plus GPU fields. */

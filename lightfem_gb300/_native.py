@@ -31,7 +31,7 @@ class SolveOptions(ctypes.Structure):
     _fields_ = [("tolerance", c_double), ("max_iterations", c_int64), ("storage", c_int32),
                 ("preconditioner", c_int32), ("precision", c_int32), ("refinement", c_int32),
                 ("inner_reduction", c_double), ("max_refinements", c_int64), ("persistent", c_int32),
-                ("reserved", c_int32)]
+                ("unrolled", c_int32)]
 
 
 class Report(ctypes.Structure):
@@ -245,10 +245,10 @@ class Context:
     @staticmethod
     def options(tolerance: float, max_iterations: int, storage: str = "csr", preconditioner: str = "jacobi",
                 precision: str = "fp64", refinement: str = "reliable", inner_reduction: float = 0.0,
-                max_refinements: int = 0, persistent: bool = False) -> SolveOptions:
+                max_refinements: int = 0, persistent: bool = False, unrolled: int = 0) -> SolveOptions:
         return SolveOptions(float(tolerance), int(max_iterations), STORAGE[storage], PRECOND[preconditioner],
                             PRECISION[precision], REFINEMENT[refinement], float(inner_reduction),
-                            int(max_refinements), int(bool(persistent)), 0)
+                            int(max_refinements), int(bool(persistent)), int(unrolled))
 
     def solve(self, options: SolveOptions, download: bool = True):
         rep = Report()

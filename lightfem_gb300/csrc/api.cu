@@ -493,6 +493,7 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
         s.inner_reduction = o->inner_reduction > 0.0 && o->inner_reduction < 1.0 ? o->inner_reduction
                                                                                  : (s.restart ? 1e-4 : 0.1);
         s.max_refinements = o->max_refinements > 0 ? o->max_refinements : 1000;
+        s.unrolled = o->unrolled > 0 ? o->unrolled : 0;
         s.rhs = h->f;
         s.x = h->u;
         s.x0 = nullptr;

@@ -71,10 +71,16 @@ struct CgArgs {
     double target, reduction;
     long long maxit, max_ref;
     int restart;
+    int use_cond;  // 0 in the unrolled profiling graph, which has no conditional nodes
     cudaGraphConditionalHandle loop, branch;
 };
 
-__device__ __forceinline__ void set_loop(const CgArgs& a, bool go) { cudaGraphSetConditional(a.loop, go ? 1u : 0u); }
+__device__ __forceinline__ void set_loop(const CgArgs& a, bool go) {
+    if (a.use_cond) cudaGraphSetConditional(a.loop, go ? 1u : 0u);
+}
+__device__ __forceinline__ void set_branch(const CgArgs& a, bool go) {
+    if (a.use_cond) cudaGraphSetConditional(a.branch, go ? 1u : 0u);
+}
 
 // Block sums of K values, then the last block to finish adds every block's sums in
 // block order and runs fin(totals) on thread 0.
@@ -492,7 +498,7 @@ __global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
     if (a.st->done) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.branch, 0u);
+        if (blockIdx.x == 0 && threadIdx.x == 0) set_branch(a, false);
         return;
     }
     const double alpha64 = a.st->alpha;
@@ -537,7 +543,7 @@ __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
                 s->rho = t[1];
             }
         }
-        cudaGraphSetConditional(a.branch, refine && !s->done ? 1u : 0u);
+        set_branch(a, refine && !s->done);
         set_loop(a, !s->done);
     });
 }
@@ -545,6 +551,7 @@ __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
 // FP64 residual replacement: r64 = f - K64 x, r32 = r64.
 template <int STORAGE>
 __global__ void __launch_bounds__(kThreads) mx_residual(CgArgs a) {
+    if (a.st->done || !a.st->refine) return;  // only reachable this way in the unrolled graph
     double v[1] = {0.0};
     if (STORAGE == LFGPU_STORAGE_CSR) {
         csr64_rows(a, [&](int c) { return a.x[c]; }, [&](int row, double y) {
@@ -588,7 +595,7 @@ __global__ void __launch_bounds__(kThreads) mx_residual(CgArgs a) {
 
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
-    if (a.st->done) return;
+    if (a.st->done || !a.st->refine) return;
     const float2* r2 = reinterpret_cast<const float2*>(a.r32);
     float2* z2 = reinterpret_cast<float2*>(a.z32);
     float rz = 0.f;
@@ -678,7 +685,35 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks) {
     add_kernel(branch, &k4, &k3, 1, mx_reprecondition<PRECOND>, blocks, a);
 }
 
+// Profiling form: the same kernels launched one by one on the stream for `iters`
+// loop passes (the branch kernels run every pass and return unless a replacement
+// is due).  Profilers see these launches; they do not descend into graph nodes.
+template <int STORAGE, int PRECOND>
+void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int iters) {
+    auto chain = [&](auto kernel) {
+        kernel<<<blocks, kThreads, 0, stream>>>(*a);
+        LF_CUDA(cudaGetLastError());
+    };
+    if (!mixed && a->x0) chain(cg64_residual<STORAGE>);
+    if (mixed) chain(mx_init<PRECOND>);
+    else chain(cg64_init<PRECOND>);
+    for (int k = 0; k < iters; ++k) {
+        if (mixed) {
+            chain(mx_product<STORAGE>);
+            chain(mx_update<PRECOND>);
+            chain(mx_residual<STORAGE>);
+            chain(mx_reprecondition<PRECOND>);
+        } else {
+            chain(cg64_product<STORAGE>);
+            chain(cg64_update<PRECOND>);
+            chain(cg64_direction);
+        }
+    }
+}
+
 }  // namespace
+
+PcgResult finish_cg(Context& c, const SolveSetup& s);
 
 PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
     const i64 n = c.n;
@@ -739,11 +774,24 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
     a.restart = s.restart;
     LF_CUDA(cudaMemsetAsync(c.cg_state.p, 0, sizeof(CgState), c.stream));
 
+    const bool csr = s.storage == LFGPU_STORAGE_CSR;
+    const bool jac = s.precond == LFGPU_PRECOND_JACOBI;
+    a.use_cond = s.unrolled > 0 ? 0 : 1;
+    if (s.unrolled > 0) {
+        LF_REQUIRE(s.unrolled <= 100000, LFGPU_ERR_ARGUMENT, "profiling runs are limited to 100000 passes");
+        const bool mx = s.mixed != 0;
+        LF_CUDA(cudaEventRecord(c.ev_a, c.stream));
+        if (csr && jac) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled);
+        else if (csr) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled);
+        else if (jac) launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled);
+        else launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled);
+        LF_CUDA(cudaEventRecord(c.ev_b, c.stream));
+        *kernel_ms = elapsed_ms(c);
+        return finish_cg(c, s);
+    }
     GraphBuilder gb{c};
     LF_CUDA(cudaGraphCreate(&gb.graph, 0));
     LF_CUDA(cudaGraphConditionalHandleCreate(&a.loop, gb.graph, 0, 0));
-    const bool csr = s.storage == LFGPU_STORAGE_CSR;
-    const bool jac = s.precond == LFGPU_PRECOND_JACOBI;
     if (!s.mixed) {
         if (csr && jac) build_fp64<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
         else if (csr) build_fp64<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
@@ -763,13 +811,21 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
     cudaGraphExecDestroy(exec);
     LF_CUDA(err);
     *kernel_ms = elapsed_ms(c);
+    return finish_cg(c, s);
+}
+
+PcgResult finish_cg(Context& c, const SolveSetup& s) {
     CgState st{};
     LF_CUDA(cudaMemcpyAsync(&st, c.cg_state.p, sizeof(st), cudaMemcpyDeviceToHost, c.stream));
     check_status(c);
-    // Kernel nodes that ran: residual (warm start) + init, then per loop pass the
-    // body (FP64: product, update, direction; mixed: product, update) and per
-    // residual replacement the two branch kernels.
-    c.launches += (s.x0 ? 1 : 0) + 1 + (s.mixed ? 2 * st.it + 2 * st.refs : 3 * st.it);
+    // Kernels that ran: residual (warm start) + init, then per loop pass the body
+    // (FP64: product, update, direction; mixed: product, update) and per residual
+    // replacement the two branch kernels; the profiling form launches every kernel
+    // of every pass.
+    if (s.unrolled > 0)
+        c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 4 : 3);
+    else
+        c.launches += (s.x0 ? 1 : 0) + 1 + (s.mixed ? 2 * st.it + 2 * st.refs : 3 * st.it);
     PcgResult r{};
     r.iterations = st.it;
     r.refinements = st.refs;

@@ -36,6 +36,7 @@ struct SolveSetup {
     const double* x0;  // FP64 warm start or nullptr (x0 = 0)
     const double* rhs; // right-hand side (device)
     double* x;         // FP64 solution (device)
+    int unrolled;      // profiling: plain graph of this many iterations instead of the conditional loop
 };
 PcgResult run_pcg(Context& c, const SolveSetup& s, float* kernel_ms);
 
