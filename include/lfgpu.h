@@ -59,7 +59,8 @@ typedef enum lfgpu_status {
     LFGPU_ERR_NONFINITE_DIAG = 10, /* non-finite diagonal in the Jacobi setup */
     LFGPU_ERR_TIMEOUT = 11,        /* a device-side wait exceeded its bound */
     LFGPU_ERR_NOMEM = 12,          /* device allocation failed */
-    LFGPU_ERR_UNSUPPORTED = 13     /* option combination not built */
+    LFGPU_ERR_UNSUPPORTED = 13,    /* option combination not built */
+    LFGPU_ERR_SCRATCH_LIMIT = 14   /* system larger than LFGPU_NOALLOC_MAX_ROWS */
 } lfgpu_status;
 
 enum { LFGPU_PLANE_STRESS = 0, LFGPU_PLANE_STRAIN = 1 };
@@ -211,6 +212,26 @@ int lfgpu_spmv(lfgpu_t h, int32_t which, int32_t storage, int32_t precision, con
  * which lambda = u and no second solve runs.  Uses the last solution. */
 int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* options,
                   double* grad, lfgpu_report* report);
+
+/* --- allocation-free residual norm (no reference counterpart) ------------------ */
+/* The reference has no counterpart: it never runs on a device.  *norm_out =
+ * ||f - K u||_2 for a CSR system held in the CALLER's device memory (row_offsets
+ * int32[n_rows + 1], columns int32[nnz], values double[nnz], u and f double[n_rows];
+ * device pointers, current device), the residual lfgpu_solve reports as
+ * true_residual.  It allocates nothing: for callers that cannot allocate device
+ * memory (work recorded into a CUDA graph capture, frameworks whose pool owns all
+ * device memory, loops where an allocation's implicit synchronisation is not
+ * acceptable).  Its only scratch is a fixed 512 KiB static device array, so
+ * n_rows <= LFGPU_NOALLOC_MAX_ROWS; larger systems return LFGPU_ERR_SCRATCH_LIMIT.
+ * The first call on a device resolves the array's address with that device
+ * current (it may load the module there): make it before any stream capture.
+ * All calls on a device share the array, which keeps the last call's contents;
+ * calls that overlap on the GPU (two streams or two threads) race on it.  Runs on
+ * `stream` (NULL: the legacy default stream) and synchronises it. */
+#define LFGPU_NOALLOC_MAX_ROWS 4194304
+int lfgpu_residual_norm_noalloc(int64_t n_rows, const int32_t* row_offsets, const int32_t* columns,
+                                const double* values, const double* u, const double* f, void* stream,
+                                double* norm_out);
 
 /* --- host utilities (setup the reference performs on the host) ----------------- */
 /* reverse_cuthill_mckee (src/reordering.cpp:11-62): node IDs in the new order. */

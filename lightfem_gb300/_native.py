@@ -19,6 +19,8 @@ OK = 0
 ERR_ARGUMENT, ERR_CUDA, ERR_STATE, ERR_JACOBIAN, ERR_EDGE, ERR_MECHANISM = 1, 2, 3, 4, 5, 6
 ERR_NOT_SPD, ERR_RHO_INITIAL, ERR_RHO, ERR_NONFINITE_DIAG, ERR_TIMEOUT, ERR_NOMEM, ERR_UNSUPPORTED = (
     7, 8, 9, 10, 11, 12, 13)
+ERR_SCRATCH_LIMIT = 14
+NOALLOC_MAX_ROWS = 4194304  # LFGPU_NOALLOC_MAX_ROWS
 ASSEMBLY = {"coloring": 0, "atomic": 1}
 STORAGE = {"csr": 0, "bsr": 1}
 PRECOND = {"jacobi": 0, "block": 1, "ic0": 2}
@@ -93,6 +95,8 @@ _SIGNATURES = {
     "lfgpu_event_elapsed": (c_int, [c_void_p, c_int32, c_int32, POINTER(c_double)]),
     "lfgpu_spmv": (c_int, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, POINTER(c_double)]),
     "lfgpu_adjoint": (c_int, [c_void_p, c_void_p, POINTER(SolveOptions), c_void_p, POINTER(Report)]),
+    "lfgpu_residual_norm_noalloc": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                            POINTER(c_double)]),
     "lfgpu_host_rcm": (c_int, [c_int64, c_void_p, c_int64, c_void_p, c_void_p]),
 }
 
@@ -132,6 +136,22 @@ def host_rcm(node_ids: np.ndarray, element_node_ids: np.ndarray) -> np.ndarray:
     if rc != OK:
         raise GpuError(rc, "RCM ordering failed: element references an unknown node ID")
     return out
+
+
+def residual_norm_noalloc(n_rows: int, row_offsets: int, columns: int, values: int, u: int, f: int,
+                          stream: int | None = None) -> float:
+    """||f - K u||_2 of a CSR system in the caller's device memory (raw device
+    pointers: int32 offsets and columns, float64 values, u and f), computed with
+    no device allocation; see lfgpu_residual_norm_noalloc in include/lfgpu.h."""
+    out = c_double()
+    rc = library().lfgpu_residual_norm_noalloc(int(n_rows), row_offsets, columns, values, u, f, stream,
+                                               ctypes.byref(out))
+    if rc == ERR_SCRATCH_LIMIT:
+        raise GpuError(rc, f"residual_norm_noalloc: {n_rows} rows exceed the static scratch limit of "
+                           f"{NOALLOC_MAX_ROWS} rows")
+    if rc != OK:
+        raise GpuError(rc, f"residual_norm_noalloc failed with status {rc}")
+    return out.value
 
 
 class Context:
