@@ -205,6 +205,14 @@ int lfgpu_event_elapsed(lfgpu_t h, int32_t slot_a, int32_t slot_b, double* ms);
 int lfgpu_spmv(lfgpu_t h, int32_t which, int32_t storage, int32_t precision, const double* x,
                double* y, int32_t repeat, double* ms_per_call);
 
+/* One FP64 application z = M^-1 r of a preconditioner of K_CONSTRAINED, built on
+ * first use: JacobiPreconditioner::apply (src/solver.cpp:497-509), the 2x2 nodal
+ * SubdomainBlockJacobi::apply (src/precond.cpp:242-291) or
+ * IncompleteCholesky0::apply (src/precond.cpp:386-412).  *ms (may be NULL) gets the
+ * device time of the application. */
+int lfgpu_apply_preconditioner(lfgpu_t h, int32_t preconditioner, const double* r, double* z,
+                               double* ms);
+
 /* --- sensitivities (no reference counterpart) ---------------------------------- */
 /* Gradient of J(u) with respect to the modulus of every element's material entry,
  * scaled per element: grad[e] = -lambda_e^T K_e u_e / E_e, with K lambda = dJ/du

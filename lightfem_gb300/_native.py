@@ -95,6 +95,7 @@ _SIGNATURES = {
     "lfgpu_event_elapsed": (c_int, [c_void_p, c_int32, c_int32, POINTER(c_double)]),
     "lfgpu_spmv": (c_int, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, POINTER(c_double)]),
     "lfgpu_adjoint": (c_int, [c_void_p, c_void_p, POINTER(SolveOptions), c_void_p, POINTER(Report)]),
+    "lfgpu_apply_preconditioner": (c_int, [c_void_p, c_int32, c_void_p, c_void_p, POINTER(c_double)]),
     "lfgpu_residual_norm_noalloc": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                             POINTER(c_double)]),
     "lfgpu_host_rcm": (c_int, [c_int64, c_void_p, c_int64, c_void_p, c_void_p]),
@@ -313,6 +314,15 @@ class Context:
         self._check(self._lib.lfgpu_spmv(self._h, which, STORAGE[storage], PRECISION[precision], _ptr(x), _ptr(y),
                                          int(repeat), ctypes.byref(ms)))
         return y, ms.value
+
+    def apply_preconditioner(self, r, preconditioner: str = "jacobi"):
+        """z = M^-1 r for the constrained K; returns (z, device ms)."""
+        r = _arr(r, np.float64)
+        z = np.empty(self.n_dofs)
+        ms = c_double()
+        self._check(self._lib.lfgpu_apply_preconditioner(self._h, PRECOND[preconditioner], _ptr(r), _ptr(z),
+                                                         ctypes.byref(ms)))
+        return z, ms.value
 
     def adjoint(self, dj_du=None, options: SolveOptions | None = None):
         grad = np.empty(self.n_elements)

@@ -236,15 +236,15 @@ int lfgpu_destroy(lfgpu_t h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto* b : {&h->mat_young, &h->mat_nu, &h->mat_t, &h->f_nodal, &h->body_bx, &h->body_by, &h->edge_a,
                     &h->edge_b, &h->prescribed, &h->K, &h->K_full, &h->f, &h->f_full, &h->bval64, &h->inv_diag64,
-                    &h->blk64, &h->u, &h->R, &h->partials, &h->scratch64, &h->l_val, &h->l_inv, &h->lt_val})
+                    &h->blk64, &h->u, &h->R, &h->partials, &h->scratch64, &h->ic0_val, &h->ic0_inv})
         b->release();
     for (auto& b : h->v64) b.release();
     for (auto& b : h->v32) b.release();
-    for (auto* b : {&h->bval32, &h->K32, &h->inv_diag32, &h->blk32, &h->l_val32, &h->l_inv32, &h->lt_val32})
+    for (auto* b : {&h->bval32, &h->K32, &h->inv_diag32, &h->blk32, &h->diag_hi, &h->diag_lo})
         b->release();
     for (auto* b : {&h->elem_mat, &h->rowptr, &h->col, &h->map, &h->diag, &h->color_elems, &h->edge_ptr,
-                    &h->edge_side, &h->edge_kind, &h->brow, &h->bcol, &h->l_ptr, &h->l_col, &h->lt_ptr,
-                    &h->lt_col, &h->lt_src, &h->fwd_rows, &h->bwd_rows})
+                    &h->edge_side, &h->edge_kind, &h->brow, &h->bcol, &h->ic0_mirror, &h->ic0_flags,
+                    &h->ic0_level})
         b->release();
     h->xy.release();
     h->elem_nodes.release();
@@ -252,6 +252,12 @@ int lfgpu_destroy(lfgpu_t h) {
     h->bar.release();
     h->status.release();
     h->pcg_result.release();
+    h->ic0_misc.release();
+    for (auto& sc : h->sched) {
+        sc.tiles.release();
+        sc.cta.release();
+    }
+    h->cg_state.release();
     for (auto& ev : h->user_ev)
         if (ev) cudaEventDestroy(ev);
     if (h->ev_a) cudaEventDestroy(h->ev_a);
@@ -479,6 +485,8 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
                    LFGPU_ERR_ARGUMENT, "preconditioner must be jacobi, block or ic0");
         LF_REQUIRE(o->precision == LFGPU_PRECISION_FP64 || o->precision == LFGPU_PRECISION_MIXED, LFGPU_ERR_ARGUMENT,
                    "precision must be fp64 or mixed");
+        LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner == LFGPU_PRECOND_IC0),
+                   LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi and block preconditioners");
         lfgpu_report r{};
         r.status = LFGPU_OK;
         const double fnorm = device_norm2(*h, h->f, h->n);
@@ -504,13 +512,13 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
         LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
         if (o->preconditioner == LFGPU_PRECOND_IC0) {
             LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
-            ensure_ic0(*h, s.mixed);
+            ensure_ic0(*h);
             LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
             r.preconditioner_setup_ms = elapsed_ms(*h);
             if (o->storage == LFGPU_STORAGE_BSR) ensure_bsr(*h);
             res = run_pcg_ic0(*h, s, &ms, &apply_ms);
             r.ic0_breakdowns = h->ic0_breakdowns;
-            r.ic0_levels = static_cast<i64>(h->fwd_level_ptr.size() + h->bwd_level_ptr.size()) - 2;
+            r.ic0_levels = h->ic0_levels;
             r.preconditioner_apply_ms = apply_ms;
         } else {
             LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
@@ -723,6 +731,30 @@ int lfgpu_spmv(lfgpu_t h, int32_t which, int32_t storage, int32_t precision, con
     });
 }
 
+int lfgpu_apply_preconditioner(lfgpu_t h, int32_t preconditioner, const double* r, double* z, double* ms) {
+    return guarded(h, [&] {
+        LF_REQUIRE(h->constrained, LFGPU_ERR_STATE, "apply boundary conditions before preconditioning");
+        LF_REQUIRE(preconditioner >= LFGPU_PRECOND_JACOBI && preconditioner <= LFGPU_PRECOND_IC0, LFGPU_ERR_ARGUMENT,
+                   "preconditioner must be jacobi, block or ic0");
+        LF_REQUIRE(r != nullptr && z != nullptr, LFGPU_ERR_ARGUMENT, "null vector");
+        const i64 n = h->n;
+        for (auto& b : h->v64) b.ensure(n);
+        Buf<double>& rd = h->v64[5];
+        Buf<double>& zd = h->v64[3];
+        LF_CUDA(cudaMemcpyAsync(rd.p, r, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+        if (preconditioner == LFGPU_PRECOND_IC0) ensure_ic0(*h);
+        else ensure_preconditioners(*h);
+        LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
+        launch_precond_apply(*h, preconditioner, rd, zd);
+        LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
+        const float t = elapsed_ms(*h);
+        check_status(*h);
+        if (ms) *ms = t;
+        LF_CUDA(cudaMemcpyAsync(z, zd.p, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+        LF_CUDA(cudaStreamSynchronize(h->stream));
+    });
+}
+
 int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, double* grad, lfgpu_report* rep) {
     return guarded(h, [&] {
         LF_REQUIRE(h->solved, LFGPU_ERR_STATE, "solve the forward problem before the adjoint");
@@ -737,6 +769,8 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
             LF_CUDA(cudaMemcpyAsync(lam.p, h->u.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
         } else {
             LF_REQUIRE(o != nullptr, LFGPU_ERR_ARGUMENT, "the adjoint solve needs solve options");
+            LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner == LFGPU_PRECOND_IC0),
+                       LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi and block preconditioners");
             // Solve K lambda = dJ/du with dJ/du zeroed on the constrained DOFs: reuse the
             // solve machinery on the adjoint right-hand side.
             std::vector<double> rhs(dj_du, dj_du + n);
@@ -770,7 +804,7 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
             double apply_ms = 0.0;
             PcgResult res;
             if (o->preconditioner == LFGPU_PRECOND_IC0) {
-                ensure_ic0(*h, s.mixed);
+                ensure_ic0(*h);
                 res = run_pcg_ic0(*h, s, &ms, &apply_ms);
             } else {
                 ensure_preconditioners(*h);

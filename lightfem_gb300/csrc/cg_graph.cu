@@ -65,6 +65,11 @@ struct CgArgs {
     float* pb;
     float* q32;
     double* partials;  // 4 slots x blocks x 4
+    const int* diag;               // IC(0): diagonal position of every row
+    const double* icf;             // IC(0) factor on the pattern of K (ic0.cu)
+    const double* icinv;           // IC(0) reciprocal pivots
+    double* y;                     // IC(0) forward-sweep result
+    unsigned long long* ic_chunks; // IC(0) row-chunk counters (forward, backward)
     int blocks;
     CgState* st;
     DeviceStatus* status;
@@ -619,6 +624,222 @@ __global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
     });
 }
 
+// ------------------------------------------------------------------ IC(0) sweeps
+// z = (L L^T)^-1 r with the factor of ic0.cu (IncompleteCholesky0::apply,
+// src/precond.cpp:386-412):
+//   forward   y(r) = (r(r) - sum_{c<r} L(r,c) y(c)) / L(r,r), rows ascending;
+//   backward  z(c) = (y(c) - sum_{r>c} L(r,c) z(r)) / L(c,c), rows descending.
+// Each term is subtracted in the reference's order -- columns ascending forward;
+// rows descending backward, the order in which the reference's column scatter
+// reaches z(c) -- without contraction, so z equals the reference's bit for bit.
+//
+// No level schedule: CTAs take 256-row chunks in sweep order from a counter, one
+// thread per row.  A value not yet written holds the kPending pattern, and a
+// thread polls (bounded) until its operand appears: in shared memory when the
+// operand's row is in the same chunk, else in global memory at GPU scope.  Chunks
+// are taken in dependency order, so the oldest unfinished row can always proceed.
+constexpr int kSweepRows = kThreads;
+constexpr unsigned long long kPending = ~0ull;  // a NaN pattern marking "not written yet"
+
+// A result that happens to carry the kPending pattern is stored as the default NaN.
+__device__ __forceinline__ unsigned long long publishable(double v) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    return b == kPending ? 0x7FF8000000000000ull : b;
+}
+
+// Bounded polls; on abort or expiry they return the kPending NaN, which poisons
+// the sweep, and the next dot product stops the solve (the status records why).
+__device__ __forceinline__ double poll_global(const double* p, DeviceStatus* status, int row) {
+    const unsigned long long* q = reinterpret_cast<const unsigned long long*>(p);
+    unsigned long long v = ld_relaxed_gpu(q);
+    if (v == kPending) {
+        const unsigned long long t0 = global_ns();
+        for (unsigned it = 1; (v = ld_relaxed_gpu(q)) == kPending; ++it)
+            if ((it & 63u) == 0u && wait_expired(status, t0, row)) break;
+    }
+    return __longlong_as_double(static_cast<long long>(v));
+}
+
+__device__ __forceinline__ double poll_shared(const volatile unsigned long long* p, DeviceStatus* status, int row) {
+    unsigned long long v = *p;
+    if (v == kPending) {
+        const unsigned long long t0 = global_ns();
+        for (unsigned it = 1; (v = *p) == kPending; ++it)
+            if ((it & 1023u) == 0u && wait_expired(status, t0, row)) break;
+    }
+    return __longlong_as_double(static_cast<long long>(v));
+}
+
+__global__ void __launch_bounds__(kSweepRows) ic0_forward(CgArgs a) {
+    if (a.st->done) return;
+    __shared__ unsigned long long s_v[kSweepRows];
+    __shared__ int s_chunk;
+    if (threadIdx.x == 0) s_chunk = static_cast<int>(atomicAdd(a.ic_chunks + 0, 1ull));
+    s_v[threadIdx.x] = kPending;
+    __syncthreads();
+    const int r0 = s_chunk * kSweepRows, row = r0 + static_cast<int>(threadIdx.x);
+    if (row >= a.n) return;
+    const int b = a.rowptr[row], d = a.diag[row];
+    double sum = a.r[row];
+    for (int k = b; k < d; ++k) {
+        const int c = ld_stream(a.col + k);
+        const double v = c >= r0 ? poll_shared(s_v + (c - r0), a.status, row) : poll_global(a.y + c, a.status, row);
+        sum = __dsub_rn(sum, __dmul_rn(ld_stream(a.icf + k), v));
+    }
+    const unsigned long long out = publishable(__dmul_rn(sum, a.icinv[row]));
+    reinterpret_cast<volatile unsigned long long*>(s_v)[threadIdx.x] = out;
+    st_relaxed_gpu(reinterpret_cast<unsigned long long*>(a.y + row), out);
+}
+
+__global__ void __launch_bounds__(kSweepRows) ic0_backward(CgArgs a) {
+    if (a.st->done) return;
+    __shared__ unsigned long long s_v[kSweepRows];
+    __shared__ int s_chunk;
+    if (threadIdx.x == 0) s_chunk = static_cast<int>(atomicAdd(a.ic_chunks + 1, 1ull));
+    s_v[threadIdx.x] = kPending;
+    __syncthreads();
+    const int top = a.n - 1 - s_chunk * kSweepRows, row = top - static_cast<int>(threadIdx.x);
+    if (row < 0) return;
+    const int d = a.diag[row];
+    double sum = a.y[row];
+    for (int k = a.rowptr[row + 1] - 1; k > d; --k) {
+        const int c = ld_stream(a.col + k);
+        const double v = c <= top ? poll_shared(s_v + (top - c), a.status, row) : poll_global(a.z + c, a.status, row);
+        sum = __dsub_rn(sum, __dmul_rn(ld_stream(a.icf + k), v));
+    }
+    const unsigned long long out = publishable(__dmul_rn(sum, a.icinv[row]));
+    reinterpret_cast<volatile unsigned long long*>(s_v)[threadIdx.x] = out;
+    st_relaxed_gpu(reinterpret_cast<unsigned long long*>(a.z + row), out);
+}
+
+__device__ __forceinline__ void ic0_mark_pending(const CgArgs& a, int i) {
+    const double pending = __longlong_as_double(static_cast<long long>(kPending));
+    reinterpret_cast<double2*>(a.y)[i] = make_double2(pending, pending);
+    reinterpret_cast<double2*>(a.z)[i] = make_double2(pending, pending);
+}
+
+__device__ __forceinline__ void ic0_reset_chunks(const CgArgs& a) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.ic_chunks[0] = 0ull;
+        a.ic_chunks[1] = 0ull;
+    }
+}
+
+// r = f (or the warm-start residual), x = x0 or 0; ||r||.
+__global__ void __launch_bounds__(kThreads) ic0_init(CgArgs a) {
+    double v[1] = {0.0};
+    double2* r2 = reinterpret_cast<double2*>(a.r);
+    double2* x2 = reinterpret_cast<double2*>(a.x);
+    const double2* f2 = reinterpret_cast<const double2*>(a.f);
+    GRID_NODES(i) {
+        const double2 rv = a.x0 ? r2[i] : f2[i];
+        r2[i] = rv;
+        x2[i] = a.x0 ? reinterpret_cast<const double2*>(a.x0)[i] : make_double2(0.0, 0.0);
+        ic0_mark_pending(a, i);
+        v[0] += rv.x * rv.x + rv.y * rv.y;
+    }
+    ic0_reset_chunks(a);
+    reduce_last<1>(a, 0, v, [&](const double* t) {
+        CgState* s = a.st;
+        s->r0 = s->rnorm = sqrt(fmax(0.0, t[0]));
+        s->it = 0;
+        if (s->r0 <= a.target) {
+            s->converged = 1;
+            s->done = 1;
+        }
+        set_loop(a, !s->done);
+    });
+}
+
+// After the first application: p = z, rho = r.z.
+__global__ void __launch_bounds__(kThreads) ic0_start(CgArgs a) {
+    if (a.st->done) return;
+    double v[1] = {0.0};
+    const double2* r2 = reinterpret_cast<const double2*>(a.r);
+    const double2* z2 = reinterpret_cast<const double2*>(a.z);
+    double2* p2 = reinterpret_cast<double2*>(a.p);
+    GRID_NODES(i) {
+        const double2 rv = r2[i], zv = z2[i];
+        p2[i] = zv;
+        v[0] += rv.x * zv.x + rv.y * zv.y;
+    }
+    reduce_last<1>(a, 3, v, [&](const double* t) {
+        CgState* s = a.st;
+        s->rho = t[0];
+        if (!(t[0] > 0.0) || !isfinite(t[0])) {
+            s->status = LFGPU_ERR_RHO_INITIAL;
+            s->done = 1;
+        }
+        set_loop(a, !s->done);
+    });
+}
+
+// x += alpha p, r -= alpha q; ||r|| decides convergence before the sweeps run.
+__global__ void __launch_bounds__(kThreads) ic0_update(CgArgs a) {
+    if (a.st->done) return;
+    const double alpha = a.st->alpha;
+    double v[1] = {0.0};
+    double2* x2 = reinterpret_cast<double2*>(a.x);
+    double2* r2 = reinterpret_cast<double2*>(a.r);
+    const double2* p2 = reinterpret_cast<const double2*>(a.p);
+    const double2* q2 = reinterpret_cast<const double2*>(a.q);
+    GRID_NODES(i) {
+        const double2 pv = p2[i], qv = q2[i];
+        double2 xv = x2[i], rv = r2[i];
+        xv.x += alpha * pv.x;
+        xv.y += alpha * pv.y;
+        rv.x -= alpha * qv.x;
+        rv.y -= alpha * qv.y;
+        x2[i] = xv;
+        r2[i] = rv;
+        ic0_mark_pending(a, i);
+        v[0] += rv.x * rv.x + rv.y * rv.y;
+    }
+    ic0_reset_chunks(a);
+    reduce_last<1>(a, 2, v, [&](const double* t) {
+        CgState* s = a.st;
+        s->it += 1;
+        s->rnorm = sqrt(fmax(0.0, t[0]));
+        if (s->rnorm <= a.target) {
+            s->converged = 1;
+            s->done = 1;
+        }
+        set_loop(a, !s->done);
+    });
+}
+
+// rho' = r.z after the sweeps; beta = rho' / rho.
+__global__ void __launch_bounds__(kThreads) ic0_dot(CgArgs a) {
+    if (a.st->done) return;
+    double v[1] = {0.0};
+    const double2* r2 = reinterpret_cast<const double2*>(a.r);
+    const double2* z2 = reinterpret_cast<const double2*>(a.z);
+    GRID_NODES(i) {
+        const double2 rv = r2[i], zv = z2[i];
+        v[0] += rv.x * zv.x + rv.y * zv.y;
+    }
+    reduce_last<1>(a, 3, v, [&](const double* t) {
+        CgState* s = a.st;
+        if (!(t[0] > 0.0) || !isfinite(t[0])) {
+            s->status = LFGPU_ERR_RHO;
+            s->done = 1;
+        } else {
+            s->beta = t[0] / s->rho;
+            s->rho = t[0];
+            if (s->it >= a.maxit) s->done = 1;
+        }
+        set_loop(a, !s->done);
+    });
+}
+
+// One FP64 application of the Jacobi or 2x2 nodal preconditioner.
+template <int PRECOND>
+__global__ void __launch_bounds__(kThreads) precond_apply_kernel(CgArgs a) {
+    const double2* r2 = reinterpret_cast<const double2*>(a.r);
+    double2* z2 = reinterpret_cast<double2*>(a.z);
+    GRID_NODES(i) { z2[i] = precond64<PRECOND>(a, i, r2[i]); }
+}
+
 // ------------------------------------------------------------------ graph assembly
 struct GraphBuilder {
     Context& c;
@@ -708,6 +929,48 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
             chain(cg64_update<PRECOND>);
             chain(cg64_direction);
         }
+    }
+}
+
+// IC(0): init -> forward -> backward -> start -> WHILE { product ; update ;
+// forward ; backward ; dot ; p update }.  The sweeps run one CTA per row chunk.
+template <int STORAGE>
+void build_ic0(cudaGraph_t g, CgArgs* a, int blocks, int chunks) {
+    cudaGraphNode_t n_res = nullptr, n_init, n_fwd, n_bwd, n_start;
+    if (a->x0) add_kernel(g, &n_res, nullptr, 0, cg64_residual<STORAGE>, blocks, a);
+    add_kernel(g, &n_init, a->x0 ? &n_res : nullptr, a->x0 ? 1 : 0, ic0_init, blocks, a);
+    add_kernel(g, &n_fwd, &n_init, 1, ic0_forward, chunks, a);
+    add_kernel(g, &n_bwd, &n_fwd, 1, ic0_backward, chunks, a);
+    add_kernel(g, &n_start, &n_bwd, 1, ic0_start, blocks, a);
+    cudaGraph_t body;
+    add_conditional(g, &n_start, 1, a->loop, cudaGraphCondTypeWhile, &body);
+    cudaGraphNode_t k[6];
+    add_kernel(body, &k[0], nullptr, 0, cg64_product<STORAGE>, blocks, a);
+    add_kernel(body, &k[1], &k[0], 1, ic0_update, blocks, a);
+    add_kernel(body, &k[2], &k[1], 1, ic0_forward, chunks, a);
+    add_kernel(body, &k[3], &k[2], 1, ic0_backward, chunks, a);
+    add_kernel(body, &k[4], &k[3], 1, ic0_dot, blocks, a);
+    add_kernel(body, &k[5], &k[4], 1, cg64_direction, blocks, a);
+}
+
+template <int STORAGE>
+void launch_ic0_unrolled(cudaStream_t stream, CgArgs* a, int blocks, int chunks, int iters) {
+    auto chain = [&](auto kernel, int grid) {
+        kernel<<<grid, kThreads, 0, stream>>>(*a);
+        LF_CUDA(cudaGetLastError());
+    };
+    if (a->x0) chain(cg64_residual<STORAGE>, blocks);
+    chain(ic0_init, blocks);
+    chain(ic0_forward, chunks);
+    chain(ic0_backward, chunks);
+    chain(ic0_start, blocks);
+    for (int k = 0; k < iters; ++k) {
+        chain(cg64_product<STORAGE>, blocks);
+        chain(ic0_update, blocks);
+        chain(ic0_forward, chunks);
+        chain(ic0_backward, chunks);
+        chain(ic0_dot, blocks);
+        chain(cg64_direction, blocks);
     }
 }
 
@@ -822,7 +1085,10 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     // (FP64: product, update, direction; mixed: product, update) and per residual
     // replacement the two branch kernels; the profiling form launches every kernel
     // of every pass.
-    if (s.unrolled > 0)
+    // IC(0): residual (warm start), init, two sweeps and start, then six kernels a pass.
+    if (s.precond == LFGPU_PRECOND_IC0)
+        c.launches += (s.x0 ? 1 : 0) + 4 + 6 * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
+    else if (s.unrolled > 0)
         c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 4 : 3);
     else
         c.launches += (s.x0 ? 1 : 0) + 1 + (s.mixed ? 2 * st.it + 2 * st.refs : 3 * st.it);
@@ -835,6 +1101,130 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     r.converged = st.converged;
     r.stagnated = st.stagnated;
     return r;
+}
+
+namespace {
+
+// Vectors and IC(0) arrays the sweeps and the solver share.
+void ic0_args(Context& c, CgArgs& a) {
+    a.diag = c.diag;
+    a.icf = c.ic0_val;
+    a.icinv = c.ic0_inv;
+    a.ic_chunks = c.ic0_misc.p + kIc0ForwardChunk;
+}
+
+}  // namespace
+
+PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double* apply_ms) {
+    const i64 n = c.n;
+    LF_REQUIRE(n % 2 == 0, LFGPU_ERR_ARGUMENT, "the GPU PCG needs an even number of DOFs (u,v pairs)");
+    LF_REQUIRE(!s.mixed, LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi and block preconditioners");
+    const int blocks = c.num_sms * (2048 / kThreads);
+    const int chunks = static_cast<int>((n + kSweepRows - 1) / kSweepRows);
+    CgArgs a{};
+    a.n = static_cast<int>(n);
+    a.nb = static_cast<int>(n / 2);
+    a.rowptr = c.rowptr;
+    a.col = c.col;
+    a.K = c.K;
+    a.f = s.rhs;
+    a.x0 = s.x0;
+    a.x = s.x;
+    for (auto& b : c.v64) b.ensure(n);
+    a.r = c.v64[0];
+    a.z = c.v64[1];
+    a.p = c.v64[2];
+    a.q = c.v64[3];
+    a.y = c.v64[4];
+    if (s.storage == LFGPU_STORAGE_BSR) {
+        ensure_bsr(c);
+        a.brow = c.brow;
+        a.bcol = c.bcol;
+        a.bval64 = reinterpret_cast<const double2*>(c.bval64.p);
+    }
+    ic0_args(c, a);
+    c.partials.ensure(static_cast<size_t>(kSlots) * kMaxReduce * blocks);
+    a.partials = c.partials;
+    a.blocks = blocks;
+    c.cg_state.ensure(sizeof(CgState));
+    a.st = reinterpret_cast<CgState*>(c.cg_state.p);
+    a.status = c.status;
+    a.target = s.tolerance;
+    a.maxit = s.max_iterations;
+    LF_CUDA(cudaMemsetAsync(c.cg_state.p, 0, sizeof(CgState), c.stream));
+    const bool csr = s.storage == LFGPU_STORAGE_CSR;
+    a.use_cond = s.unrolled > 0 ? 0 : 1;
+    if (s.unrolled > 0) {
+        LF_REQUIRE(s.unrolled <= 100000, LFGPU_ERR_ARGUMENT, "profiling runs are limited to 100000 passes");
+        LF_CUDA(cudaEventRecord(c.ev_a, c.stream));
+        if (csr) launch_ic0_unrolled<LFGPU_STORAGE_CSR>(c.stream, &a, blocks, chunks, s.unrolled);
+        else launch_ic0_unrolled<LFGPU_STORAGE_BSR>(c.stream, &a, blocks, chunks, s.unrolled);
+        LF_CUDA(cudaEventRecord(c.ev_b, c.stream));
+        *kernel_ms = elapsed_ms(c);
+    } else {
+        GraphBuilder gb{c};
+        LF_CUDA(cudaGraphCreate(&gb.graph, 0));
+        LF_CUDA(cudaGraphConditionalHandleCreate(&a.loop, gb.graph, 0, 0));
+        if (csr) build_ic0<LFGPU_STORAGE_CSR>(gb.graph, &a, blocks, chunks);
+        else build_ic0<LFGPU_STORAGE_BSR>(gb.graph, &a, blocks, chunks);
+        cudaGraphExec_t exec = nullptr;
+        LF_CUDA(cudaGraphInstantiate(&exec, gb.graph, 0));
+        cudaError_t err = cudaEventRecord(c.ev_a, c.stream);
+        if (err == cudaSuccess) err = cudaGraphLaunch(exec, c.stream);
+        if (err == cudaSuccess) err = cudaEventRecord(c.ev_b, c.stream);
+        cudaGraphExecDestroy(exec);
+        LF_CUDA(err);
+        *kernel_ms = elapsed_ms(c);
+    }
+    PcgResult res = finish_cg(c, s);
+    // Time one standalone application (forward + backward sweep) on the final
+    // residual; the solve made iterations + 1 of them.
+    LF_CUDA(cudaEventRecord(c.ev_a, c.stream));
+    launch_precond_apply(c, LFGPU_PRECOND_IC0, c.v64[0], c.v64[5]);
+    LF_CUDA(cudaEventRecord(c.ev_b, c.stream));
+    const double one = elapsed_ms(c);
+    check_status(c);
+    if (apply_ms) *apply_ms = one * static_cast<double>(res.iterations + 1);
+    return res;
+}
+
+void launch_precond_apply(Context& c, int precond, const double* r, double* z) {
+    const i64 n = c.n;
+    LF_REQUIRE(n % 2 == 0, LFGPU_ERR_ARGUMENT, "the GPU preconditioners need an even number of DOFs (u,v pairs)");
+    const int blocks = c.num_sms * (2048 / kThreads);
+    CgArgs a{};
+    a.n = static_cast<int>(n);
+    a.nb = static_cast<int>(n / 2);
+    a.rowptr = c.rowptr;
+    a.col = c.col;
+    a.r = const_cast<double*>(r);
+    a.z = z;
+    a.status = c.status;
+    a.invd64 = c.inv_diag64;
+    a.blk64 = c.blk64;
+    if (precond == LFGPU_PRECOND_IC0) {
+        // The sweeps read the done flag of a solver state: give them a fresh one.
+        c.cg_state.ensure(sizeof(CgState));
+        a.st = reinterpret_cast<CgState*>(c.cg_state.p);
+        LF_CUDA(cudaMemsetAsync(c.cg_state.p, 0, sizeof(CgState), c.stream));
+        c.v64[4].ensure(n);
+        a.y = c.v64[4];
+        ic0_args(c, a);
+        LF_CUDA(cudaMemsetAsync(a.y, 0xFF, sizeof(double) * n, c.stream));
+        LF_CUDA(cudaMemsetAsync(z, 0xFF, sizeof(double) * n, c.stream));
+        LF_CUDA(cudaMemsetAsync(a.ic_chunks, 0, 2 * sizeof(unsigned long long), c.stream));
+        const int chunks = static_cast<int>((n + kSweepRows - 1) / kSweepRows);
+        ic0_forward<<<chunks, kSweepRows, 0, c.stream>>>(a);
+        ic0_backward<<<chunks, kSweepRows, 0, c.stream>>>(a);
+        c.launches += 2;
+    } else if (precond == LFGPU_PRECOND_JACOBI) {
+        precond_apply_kernel<LFGPU_PRECOND_JACOBI><<<blocks, kThreads, 0, c.stream>>>(a);
+        c.launches += 1;
+    } else {
+        precond_apply_kernel<LFGPU_PRECOND_BLOCK2><<<blocks, kThreads, 0, c.stream>>>(a);
+        c.launches += 1;
+    }
+    LF_CUDA(cudaGetLastError());
 }
 
 }  // namespace lfgpu

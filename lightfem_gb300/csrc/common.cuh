@@ -174,13 +174,15 @@ struct Context {
     unsigned long long pattern_version = 0;
     std::vector<int> h_brow;
 
-    // ic0 state (built per K version)
-    unsigned long long ic0_version = ~0ull;
-    Buf<int> l_ptr, l_col, lt_ptr, lt_col, lt_src, fwd_rows, bwd_rows;
-    Buf<double> l_val, l_inv, lt_val;
-    Buf<float> l_val32, l_inv32, lt_val32;
-    std::vector<int> fwd_level_ptr, bwd_level_ptr;
-    i64 ic0_breakdowns = 0;
+    // IC(0) factor on the pattern of K (ic0.cu): left of the diagonal L(r, c), on
+    // it the pivot, right of it L(c, r).  Built per K version; the mirror map (for
+    // every upper entry, the index of its lower twin) per pattern version.
+    unsigned long long ic0_version = ~0ull, ic0_pattern_version = ~0ull;
+    Buf<double> ic0_val, ic0_inv;
+    Buf<int> ic0_mirror, ic0_flags, ic0_level;
+    Buf<unsigned long long> ic0_misc;  // see kIc0* slots in ic0.cu
+    unsigned int ic0_epoch = 0;
+    i64 ic0_breakdowns = 0, ic0_levels = 0;
 
     lfgpu_timings timings{};
     i64 launches = 0;                 // kernels launched by this handle (graph nodes included)
@@ -220,6 +222,41 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 // A wait that gives up after this long sets DeviceStatus::abort and returns.
 constexpr unsigned long long kWaitLimitNs = 4000000000ull;  // 4 s
+
+// GPU-scope accesses for values and flags that other CTAs poll while a kernel runs.
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_gpu(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_gpu(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_relaxed_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// True when a bounded wait started at t0 must stop: another CTA aborted, or the
+// limit ran out (then this wait records LFGPU_ERR_TIMEOUT and sets the abort flag).
+__device__ __forceinline__ bool wait_expired(DeviceStatus* status, unsigned long long t0, int index) {
+    if (ld_relaxed_gpu(&status->abort) != 0u) return true;
+    if (global_ns() - t0 > kWaitLimitNs) {
+        atomicExch(&status->abort, 1u);
+        record_failure(status, LFGPU_ERR_TIMEOUT, index);
+        return true;
+    }
+    return false;
+}
 
 // Grid-wide barrier for cooperative launches, bounded in time.  Every CTA arrives
 // with a release add on a monotonically increasing counter and waits (acquire)

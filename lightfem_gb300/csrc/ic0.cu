@@ -1,14 +1,199 @@
-// Incomplete Cholesky IC(0) on the GPU (placeholder until the level-scheduled
-// factorisation and sweeps land).
+// Incomplete Cholesky IC(0) of the constrained K on the GPU: the factorisation
+// (IncompleteCholesky0, src/precond.cpp:298-384).  The triangular sweeps that
+// apply the factor run inside the PCG graph (cg_graph.cu).
+//
+// Storage.  The factor lives on the pattern of K.  In row r the entries left of
+// the diagonal hold L(r, c), the diagonal holds the pivot L(r, r), and the entries
+// right of it hold L(c, r) -- the transpose -- so the forward sweep reads the left
+// part of each row and the backward sweep the right part, both as contiguous row
+// segments of one array.  This needs a structurally symmetric pattern, which Q4
+// assembly always produces; the setup checks that every entry right of a diagonal
+// has its twin left of the other row's diagonal.
+//
+// Factorisation.  Row r needs the finished rows c < r it references.  Warps take
+// 32-row chunks from a counter in increasing row order; each thread factorises one
+// row and waits (bounded) on a per-row flag for every row it references, so a row
+// proceeds as soon as its dependencies are done -- no level schedule.  Each row is
+// computed by one thread in the reference's operation order without contraction,
+// so the factor equals the reference's bit for bit.
 #include "common.cuh"
 #include "kernels.hpp"
 
+#include <climits>
+#include <cmath>
+
 namespace lfgpu {
+namespace {
 
-void ensure_ic0(Context&, bool) { throw Error{LFGPU_ERR_UNSUPPORTED, "ic0 is not built yet"}; }
+constexpr int kThreads = 256;
 
-PcgResult run_pcg_ic0(Context&, const SolveSetup&, float*, double*) {
-    throw Error{LFGPU_ERR_UNSUPPORTED, "ic0 is not built yet"};
+// For every entry right of the diagonal of row c (column r > c): the index of the
+// entry (r, c) left of the diagonal of row r.  A missing twin records
+// LFGPU_ERR_ARGUMENT with the row.
+__global__ void ic0_mirror_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                  const int* __restrict__ diag, int* __restrict__ mirror, DeviceStatus* status) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const int d = diag[c], e = rowptr[c + 1];
+        for (int k = d + 1; k < e; ++k) {
+            const int r = col[k];
+            int lo = rowptr[r], hi = diag[r];
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (col[mid] < c) lo = mid + 1;
+                else hi = mid;
+            }
+            const bool found = lo < diag[r] && col[lo] == c;
+            mirror[k] = found ? lo : -1;
+            if (!found) record_failure(status, LFGPU_ERR_ARGUMENT, c);
+        }
+    }
+}
+
+// max_r |K(r, r)| (the pivot floor's scale, src/precond.cpp:334-338).
+__global__ void ic0_scale_kernel(int n, const int* __restrict__ diag, const double* __restrict__ K,
+                                 unsigned long long* misc) {
+    double m = 0.0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+        m = fmax(m, fabs(K[diag[r]]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&misc[kIc0Scale], static_cast<unsigned long long>(__double_as_longlong(m)));
+}
+
+// Bounded wait until row c's flag shows this factorisation's epoch.
+__device__ __forceinline__ bool wait_row(const int* flag, int epoch, DeviceStatus* status, int row) {
+    if (ld_acquire_gpu(flag) == epoch) return true;
+    const unsigned long long t0 = global_ns();
+    for (unsigned it = 1;; ++it) {
+        if (ld_acquire_gpu(flag) == epoch) return true;
+        if ((it & 63u) == 0u && wait_expired(status, t0, row)) return false;
+    }
+}
+
+// Row r of the factor (src/precond.cpp:344-382): for each c < r in the row,
+// L(r,c) = (K(r,c) - sum_j L(r,j) L(c,j)) / L(c,c) over the common columns j < c,
+// then L(r,r) = sqrt(K(r,r) - sum_c L(r,c)^2), with a non-positive or non-finite
+// value replaced by the floor.
+__device__ __forceinline__ void factor_row(int r, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                           const int* __restrict__ diag, const double* __restrict__ K, double* F,
+                                           double* inv, int* flags, int* level, int epoch, double floor_value,
+                                           unsigned long long* misc, DeviceStatus* status) {
+    const int b = rowptr[r], d = diag[r];
+    int lev = 0;
+    for (int k = b; k < d; ++k) {
+        const int c = col[k];
+        wait_row(flags + c, epoch, status, r);  // on expiry the row is finished with whatever is there
+        lev = max(lev, __ldcg(level + c) + 1);
+        double sum = K[k];
+        int p = b, q = rowptr[c];
+        const int qe = diag[c];
+        while (p < k && q < qe) {
+            const int cp = col[p], cq = col[q];
+            if (cp < cq) {
+                ++p;
+            } else if (cp > cq) {
+                ++q;
+            } else {
+                sum = __dsub_rn(sum, __dmul_rn(F[p], __ldcg(F + q)));
+                ++p;
+                ++q;
+            }
+        }
+        F[k] = __dmul_rn(sum, __ldcg(inv + c));
+    }
+    double sum = K[d];
+    for (int k = b; k < d; ++k) sum = __dsub_rn(sum, __dmul_rn(F[k], F[k]));
+    if (!(sum > 0.0) || !isfinite(sum)) {
+        atomicAdd(&misc[kIc0Breakdowns], 1ull);
+        sum = floor_value;
+    }
+    const double pivot = __dsqrt_rn(sum);
+    F[d] = pivot;
+    inv[r] = __ddiv_rn(1.0, pivot);
+    level[r] = lev;
+    atomicMax(&misc[kIc0MaxLevel], static_cast<unsigned long long>(lev));
+    __threadfence();
+    st_release_gpu(flags + r, epoch);
+}
+
+__global__ void __launch_bounds__(kThreads) ic0_factor_kernel(int n, const int* __restrict__ rowptr,
+                                                              const int* __restrict__ col,
+                                                              const int* __restrict__ diag,
+                                                              const double* __restrict__ K, double* F, double* inv,
+                                                              int* flags, int* level, int epoch,
+                                                              unsigned long long* misc, DeviceStatus* status) {
+    const int lane = threadIdx.x & 31;
+    const double scale = __longlong_as_double(static_cast<long long>(misc[kIc0Scale]));
+    const double floor_value = fmax(1.0e-30, 1.0e-14 * scale);
+    while (true) {
+        int base = 0;
+        if (lane == 0) base = static_cast<int>(atomicAdd(&misc[kIc0FactorChunk], 32ull));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const int r = base + lane;
+        if (r < n) factor_row(r, rowptr, col, diag, K, F, inv, flags, level, epoch, floor_value, misc, status);
+        __syncwarp();
+    }
+}
+
+// Right of each diagonal: copy L(c, r) from its twin.
+__global__ void ic0_transpose_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ diag,
+                                     const int* __restrict__ mirror, double* F) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        const int e = rowptr[c + 1];
+        for (int k = diag[c] + 1; k < e; ++k) F[k] = F[mirror[k]];
+    }
+}
+
+}  // namespace
+
+void ensure_ic0(Context& c) {
+    if (c.ic0_version == c.k_version) return;
+    LF_REQUIRE(c.n > 0 && c.n < INT_MAX / 2, LFGPU_ERR_ARGUMENT, "ic0: system size out of range");
+    const int n = static_cast<int>(c.n);
+    const int grid = grid_for(n, kThreads, 16 * c.num_sms);
+    c.ic0_misc.ensure(kIc0Slots);
+    if (c.ic0_pattern_version != c.pattern_version) {
+        c.ic0_mirror.ensure(c.nnz);
+        c.ic0_flags.ensure(n);
+        c.ic0_level.ensure(n);
+        LF_CUDA(cudaMemsetAsync(c.ic0_flags.p, 0, sizeof(int) * n, c.stream));
+        c.ic0_epoch = 0;
+        ic0_mirror_kernel<<<grid, kThreads, 0, c.stream>>>(n, c.rowptr, c.col, c.diag, c.ic0_mirror, c.status);
+        c.launches += 1;
+        LF_CUDA(cudaGetLastError());
+        try {
+            check_status(c);
+        } catch (const Error& e) {
+            if (e.code != LFGPU_ERR_ARGUMENT) throw;
+            throw Error{LFGPU_ERR_ARGUMENT, "ic0 needs a structurally symmetric pattern"};
+        }
+        c.ic0_pattern_version = c.pattern_version;
+    }
+    c.ic0_val.ensure(c.nnz);
+    c.ic0_inv.ensure(n);
+    if (c.ic0_epoch >= static_cast<unsigned>(INT_MAX)) {
+        LF_CUDA(cudaMemsetAsync(c.ic0_flags.p, 0, sizeof(int) * n, c.stream));
+        c.ic0_epoch = 0;
+    }
+    const int epoch = static_cast<int>(++c.ic0_epoch);
+    LF_CUDA(cudaMemsetAsync(c.ic0_misc.p, 0, sizeof(unsigned long long) * kIc0Slots, c.stream));
+    ic0_scale_kernel<<<grid, kThreads, 0, c.stream>>>(n, c.diag, c.K, c.ic0_misc);
+    // Every thread may wait on rows other warps hold, so the grid stays within one
+    // resident wave; warps take further chunks from the counter.
+    const int resident = c.num_sms * (2048 / kThreads);
+    ic0_factor_kernel<<<std::min(resident, grid_for(n, kThreads)), kThreads, 0, c.stream>>>(
+        n, c.rowptr, c.col, c.diag, c.K, c.ic0_val, c.ic0_inv, c.ic0_flags, c.ic0_level, epoch, c.ic0_misc, c.status);
+    ic0_transpose_kernel<<<grid, kThreads, 0, c.stream>>>(n, c.rowptr, c.diag, c.ic0_mirror, c.ic0_val);
+    c.launches += 3;
+    LF_CUDA(cudaGetLastError());
+    unsigned long long misc[kIc0Slots];
+    LF_CUDA(cudaMemcpyAsync(misc, c.ic0_misc.p, sizeof(misc), cudaMemcpyDeviceToHost, c.stream));
+    check_status(c);
+    c.ic0_breakdowns = static_cast<i64>(misc[kIc0Breakdowns]);
+    // The forward and the backward sweep each have (longest chain + 1) levels.
+    c.ic0_levels = 2 * (static_cast<i64>(misc[kIc0MaxLevel]) + 1);
+    c.ic0_version = c.k_version;
 }
 
 }  // namespace lfgpu

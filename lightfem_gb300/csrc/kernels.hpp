@@ -42,10 +42,23 @@ PcgResult run_pcg(Context& c, const SolveSetup& s, float* kernel_ms);
 
 // cg_graph.cu: the same solver as a device-driven CUDA graph of per-phase kernels
 PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms);
-
-// ic0.cu
-void ensure_ic0(Context& c, bool fp32);
+// FP64 PCG with the IC(0) factor (triangular sweeps inside the graph); apply_ms is
+// the device time of one standalone application times the applications made.
 PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double* apply_ms);
+// One FP64 application z = M^-1 r of the built preconditioner, on the stream.
+void launch_precond_apply(Context& c, int precond, const double* r, double* z);
+
+// ic0.cu: IC(0) factor of the constrained K on its own pattern (built per K version)
+enum Ic0Slot {
+    kIc0Scale = 0,     // max |K(r, r)| as double bits (atomicMax)
+    kIc0Breakdowns,    // pivots replaced by the floor
+    kIc0MaxLevel,      // longest dependency chain of the factor, in rows
+    kIc0FactorChunk,   // row-chunk counters of the factorisation and of the two sweeps
+    kIc0ForwardChunk,
+    kIc0BackwardChunk,
+    kIc0Slots = 8
+};
+void ensure_ic0(Context& c);
 
 // adjoint.cu
 void launch_adjoint_grad(Context& c, const double* u, const double* lam, double* grad);

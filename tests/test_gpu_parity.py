@@ -17,7 +17,7 @@ from lightfem_gb300.solver import LinearElasticSolver, upload_model
 
 pytestmark = pytest.mark.gpu
 
-GPU_VARIANTS = ["csr_jacobi", "bsr_jacobi", "bsr_block1", "csr_block1"]
+GPU_VARIANTS = ["csr_jacobi", "bsr_jacobi", "bsr_block1", "csr_block1", "csr_ic0", "bsr_ic0"]
 
 
 def rel(a, b):
@@ -130,7 +130,7 @@ def test_cfg1_full_size(native, golden_json):
     """The 200x200 workload against the reference's iteration counts and fields."""
     g = load_golden("cfg1")
     ref = golden_json["cfg1"]
-    for variant in ("csr_jacobi", "bsr_jacobi", "bsr_block1"):
+    for variant in ("csr_jacobi", "bsr_jacobi", "bsr_block1", "csr_ic0"):
         storage, precond, _, _ = VARIANTS[variant]
         model = indexed(mesh.workload(1))
         model.settings.storage, model.settings.preconditioner = storage, precond
@@ -159,6 +159,34 @@ def test_mixed_precision_reaches_fp64_target(native, storage, precond, refinemen
     # Two solutions at a 1e-8 relative residual differ by at most cond(K) * 1e-8;
     # the FP64 solution is the oracle here.
     assert rel(res.displacement, fp64.displacement) <= 1e-4
+
+
+@pytest.mark.parametrize("name", ["grid6", "beam", "strain"])
+def test_preconditioner_applications(native, oracle, name):
+    """z = M^-1 f_c on the device equals the oracle's on the same constrained K bit
+    for bit (Jacobi, 2x2 nodal blocks, IC(0) factor and sweeps), and the reference's
+    golden z within the assembly tolerance (K itself differs at rounding level)."""
+    g = load_golden(name)
+    model, ctx = prepared(native, name)
+    ctx.assemble("coloring")
+    ctx.apply_dirichlet()
+    Kc = ctx.download(native.K_CONSTRAINED)
+    fc = ctx.download(native.F_CONSTRAINED)
+    rp, col, _, _ = ctx.download_pattern()
+    golden_block = g["z_block1"] if name == "grid6" else g["z_block"]
+    for precond, golden in (("jacobi", g["z_jacobi"]), ("block", golden_block), ("ic0", g["z_ic0"])):
+        z, ms = ctx.apply_preconditioner(fc, precond)
+        z_ref, _ = oracle.precond_apply(rp, col, Kc, fc, precond, "chunk", 1)
+        np.testing.assert_array_equal(z, z_ref, err_msg=precond)
+        assert rel(z, golden) <= 1e-10, precond
+        assert ms > 0.0
+
+
+def test_ic0_rejects_mixed_precision(native):
+    model = indexed(CASES["grid6"]())
+    model.settings.preconditioner, model.settings.precision = "ic0", "mixed"
+    with pytest.raises(RuntimeError, match="mixed precision supports the jacobi and block"):
+        LinearElasticSolver().solve(model)
 
 
 def test_spmv_products(native, oracle):
