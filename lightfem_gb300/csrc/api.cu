@@ -778,11 +778,9 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
             LF_CUDA(cudaMemcpy(fixed.data(), h->fixed.p, n, cudaMemcpyDeviceToHost));
             for (i64 i = 0; i < n; ++i)
                 if (fixed[i]) rhs[i] = 0.0;
-            Buf<double>& b = h->f_nodal;  // staging: the adjoint rhs lives beside the forward data
             Buf<double> adj_rhs;
             adj_rhs.ensure(n);
             LF_CUDA(cudaMemcpyAsync(adj_rhs.p, rhs.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
-            (void)b;
             const double rnorm = [&] {
                 double s = 0.0;
                 for (double v : rhs) s += v * v;
