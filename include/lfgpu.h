@@ -119,10 +119,14 @@ typedef struct lfgpu_report {
     int64_t ic0_breakdowns;          /* ic0: clamped pivots */
     int64_t ic0_levels;              /* ic0: forward + backward level count */
     int64_t fallback_fp64;           /* mixed: 1 if the FP32 inner solve stagnated and FP64 PCG finished */
-    /* Time inside the persistent PCG kernel as CTA 0 sees it, summed over iterations:
-     * [0] product phase, [1] grid sum after it, [2] update phase, [3] grid sum after
-     * it, [4] FP64: p update / mixed: residual replacements, [5] FP64: barrier after
-     * the p update.  matvec_ms equals phase_ms[0]. */
+    /* Persistent kernel: time as CTA 0 sees it, summed over iterations: [0] product
+     * phase, [1] grid sum after it, [2] update phase, [3] grid sum after it, [4] FP64:
+     * p update / mixed: residual replacements, [5] FP64: barrier after the p update.
+     * Profiling run (unrolled > 0, up to 5000 passes): device time of each kernel
+     * kind summed over the passes (CUDA events between launches): [0] product,
+     * [1] update, [2] FP64 p update / mixed residual replacement / IC(0) forward
+     * sweep, [3] mixed re-preconditioning / IC(0) backward sweep, [4] IC(0) r.z,
+     * [5] IC(0) p update.  Graph runs leave it zero.  matvec_ms equals phase_ms[0]. */
     double phase_ms[6];
 } lfgpu_report;
 

@@ -236,7 +236,8 @@ int lfgpu_destroy(lfgpu_t h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto* b : {&h->mat_young, &h->mat_nu, &h->mat_t, &h->f_nodal, &h->body_bx, &h->body_by, &h->edge_a,
                     &h->edge_b, &h->prescribed, &h->K, &h->K_full, &h->f, &h->f_full, &h->bval64, &h->inv_diag64,
-                    &h->blk64, &h->u, &h->R, &h->partials, &h->scratch64, &h->ic0_val, &h->ic0_inv})
+                    &h->blk64, &h->u, &h->R, &h->partials, &h->scratch64, &h->ic0_val, &h->ic0_inv, &h->lam,
+                    &h->adj_rhs})
         b->release();
     for (auto& b : h->v64) b.release();
     for (auto& b : h->v32) b.release();
@@ -472,6 +473,28 @@ int lfgpu_apply_dirichlet(lfgpu_t h) {
     });
 }
 
+namespace {
+
+// The FP32 inner solve of a mixed solve stopped making progress: finish with FP64
+// PCG warm-started from its solution s.x.  Adds the device time to *ms.
+lfgpu::PcgResult finish_in_fp64(lfgpu_t h, const lfgpu_solve_options* o, const lfgpu::SolveSetup& s,
+                                lfgpu::i64 done_iterations, double* ms) {
+    using namespace lfgpu;
+    Buf<double>& x0 = h->v64[5];
+    x0.ensure(h->n);
+    LF_CUDA(cudaMemcpyAsync(x0.p, s.x, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->stream));
+    SolveSetup f = s;
+    f.mixed = 0;
+    f.x0 = x0.p;
+    f.max_iterations = std::max<i64>(1, s.max_iterations - done_iterations);
+    float ms2 = 0.f;
+    const PcgResult r2 = o->persistent ? run_pcg(*h, f, &ms2) : run_cg_graph(*h, f, &ms2);
+    *ms += ms2;
+    return r2;
+}
+
+}  // namespace
+
 int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_report* rep) {
     return guarded(h, [&] {
         LF_REQUIRE(o != nullptr, LFGPU_ERR_ARGUMENT, "null solve options");
@@ -542,20 +565,7 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
         for (int k = 0; k < 6; ++k) r.phase_ms[k] = static_cast<double>(res.phase_ns[k]) * 1e-6;
         r.matvec_ms = r.phase_ms[0];
         if (s.mixed && res.stagnated && res.status == LFGPU_OK) {
-            // The FP32 inner solve stopped making progress: finish in FP64 from the
-            // current solution.
-            h->scratch64.ensure(64);
-            Buf<double>& x0 = h->v64[5];
-            x0.ensure(h->n);
-            LF_CUDA(cudaMemcpyAsync(x0.p, h->u.p, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->stream));
-            SolveSetup f = s;
-            f.mixed = 0;
-            f.x0 = x0.p;
-            f.max_iterations = std::max<i64>(1, o->max_iterations - res.iterations);
-            float ms2 = 0.f;
-            PcgResult r2 = o->preconditioner == LFGPU_PRECOND_IC0 ? run_pcg_ic0(*h, f, &ms2, &apply_ms)
-                                                                  : (o->persistent ? run_pcg(*h, f, &ms2) : run_cg_graph(*h, f, &ms2));
-            total_ms += ms2;
+            const PcgResult r2 = finish_in_fp64(h, o, s, res.iterations, &total_ms);
             r.iterations += r2.iterations;
             r.final_residual = r2.final_residual;
             r.converged = r2.converged;
@@ -760,7 +770,7 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
         LF_REQUIRE(h->solved, LFGPU_ERR_STATE, "solve the forward problem before the adjoint");
         LF_REQUIRE(grad != nullptr, LFGPU_ERR_ARGUMENT, "null gradient output");
         const i64 n = h->n;
-        Buf<double>& lam = h->v64[5];
+        Buf<double>& lam = h->lam;
         lam.ensure(n);
         Buf<double>& g = h->scratch64;
         lfgpu_report r{};
@@ -778,7 +788,7 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
             LF_CUDA(cudaMemcpy(fixed.data(), h->fixed.p, n, cudaMemcpyDeviceToHost));
             for (i64 i = 0; i < n; ++i)
                 if (fixed[i]) rhs[i] = 0.0;
-            Buf<double> adj_rhs;
+            Buf<double>& adj_rhs = h->adj_rhs;
             adj_rhs.ensure(n);
             LF_CUDA(cudaMemcpyAsync(adj_rhs.p, rhs.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
             const double rnorm = [&] {
@@ -808,15 +818,24 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
                 ensure_preconditioners(*h);
                 res = o->persistent ? run_pcg(*h, s, &ms) : run_cg_graph(*h, s, &ms);
             }
-            adj_rhs.release();
+            double total_ms = ms;
             r.iterations = res.iterations;
             r.refinements = res.refinements;
             r.initial_residual = res.initial_residual;
             r.final_residual = res.final_residual;
             r.converged = res.converged;
             r.status = res.status;
-            r.solve_ms = ms;
-            LF_REQUIRE(res.status == LFGPU_OK, res.status, "adjoint PCG failed");
+            if (s.mixed && res.stagnated && res.status == LFGPU_OK) {
+                const PcgResult r2 = finish_in_fp64(h, o, s, res.iterations, &total_ms);
+                r.iterations += r2.iterations;
+                r.final_residual = r2.final_residual;
+                r.converged = r2.converged;
+                r.status = r2.status;
+                r.fallback_fp64 = 1;
+            }
+            r.solve_ms = total_ms;
+            LF_REQUIRE(r.status == LFGPU_OK, r.status, "adjoint PCG failed");
+            LF_REQUIRE(r.converged, LFGPU_ERR_STATE, "adjoint PCG did not converge");
         }
         g.ensure(64 + static_cast<size_t>(h->n_elem));
         double* gd = g.p + 64;

@@ -22,11 +22,13 @@
 #include "kernels.hpp"
 
 #include <cmath>
+#include <vector>
 
 namespace lfgpu {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kTimedPasses = 5000;  // profiling runs up to this long time every launch
 
 struct CgState {
     double rho, alpha, beta, r0, rnorm, rmax, rtrue, rtrue_prev;
@@ -906,28 +908,62 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks) {
     add_kernel(branch, &k4, &k3, 1, mx_reprecondition<PRECOND>, blocks, a);
 }
 
+// Per-kernel device time of the profiling form: an event after every launch; the
+// time between consecutive events is charged to that launch's phase slot.
+struct EventTrail {
+    cudaStream_t stream;
+    bool on;
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> slot;
+    EventTrail(cudaStream_t s, bool enabled) : stream(s), on(enabled) { mark(-1); }
+    ~EventTrail() {
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    }
+    void mark(int phase) {
+        if (!on) return;
+        cudaEvent_t e;
+        LF_CUDA(cudaEventCreate(&e));
+        ev.push_back(e);
+        slot.push_back(phase);
+        LF_CUDA(cudaEventRecord(e, stream));
+    }
+    void totals(unsigned long long (&ns)[6]) {
+        for (auto& v : ns) v = 0;
+        if (!on || ev.size() < 2) return;
+        LF_CUDA(cudaEventSynchronize(ev.back()));
+        for (size_t i = 1; i < ev.size(); ++i) {
+            float ms = 0.f;
+            LF_CUDA(cudaEventElapsedTime(&ms, ev[i - 1], ev[i]));
+            if (slot[i] >= 0 && slot[i] < 6) ns[slot[i]] += static_cast<unsigned long long>(ms * 1.0e6);
+        }
+    }
+};
+
 // Profiling form: the same kernels launched one by one on the stream for `iters`
 // loop passes (the branch kernels run every pass and return unless a replacement
 // is due).  Profilers see these launches; they do not descend into graph nodes.
+// Phase slots: 0 product, 1 update, 2 FP64 p update or mixed residual
+// replacement, 3 mixed re-preconditioning.
 template <int STORAGE, int PRECOND>
-void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int iters) {
-    auto chain = [&](auto kernel) {
+void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int iters, EventTrail& trail) {
+    auto chain = [&](auto kernel, int phase) {
         kernel<<<blocks, kThreads, 0, stream>>>(*a);
         LF_CUDA(cudaGetLastError());
+        trail.mark(phase);
     };
-    if (!mixed && a->x0) chain(cg64_residual<STORAGE>);
-    if (mixed) chain(mx_init<PRECOND>);
-    else chain(cg64_init<PRECOND>);
+    if (!mixed && a->x0) chain(cg64_residual<STORAGE>, -1);
+    if (mixed) chain(mx_init<PRECOND>, -1);
+    else chain(cg64_init<PRECOND>, -1);
     for (int k = 0; k < iters; ++k) {
         if (mixed) {
-            chain(mx_product<STORAGE>);
-            chain(mx_update<PRECOND>);
-            chain(mx_residual<STORAGE>);
-            chain(mx_reprecondition<PRECOND>);
+            chain(mx_product<STORAGE>, 0);
+            chain(mx_update<PRECOND>, 1);
+            chain(mx_residual<STORAGE>, 2);
+            chain(mx_reprecondition<PRECOND>, 3);
         } else {
-            chain(cg64_product<STORAGE>);
-            chain(cg64_update<PRECOND>);
-            chain(cg64_direction);
+            chain(cg64_product<STORAGE>, 0);
+            chain(cg64_update<PRECOND>, 1);
+            chain(cg64_direction, 2);
         }
     }
 }
@@ -953,24 +989,27 @@ void build_ic0(cudaGraph_t g, CgArgs* a, int blocks, int chunks) {
     add_kernel(body, &k[5], &k[4], 1, cg64_direction, blocks, a);
 }
 
+// Phase slots: 0 product, 1 update, 2 forward sweep, 3 backward sweep, 4 r.z,
+// 5 p update.
 template <int STORAGE>
-void launch_ic0_unrolled(cudaStream_t stream, CgArgs* a, int blocks, int chunks, int iters) {
-    auto chain = [&](auto kernel, int grid) {
+void launch_ic0_unrolled(cudaStream_t stream, CgArgs* a, int blocks, int chunks, int iters, EventTrail& trail) {
+    auto chain = [&](auto kernel, int grid, int phase) {
         kernel<<<grid, kThreads, 0, stream>>>(*a);
         LF_CUDA(cudaGetLastError());
+        trail.mark(phase);
     };
-    if (a->x0) chain(cg64_residual<STORAGE>, blocks);
-    chain(ic0_init, blocks);
-    chain(ic0_forward, chunks);
-    chain(ic0_backward, chunks);
-    chain(ic0_start, blocks);
+    if (a->x0) chain(cg64_residual<STORAGE>, blocks, -1);
+    chain(ic0_init, blocks, -1);
+    chain(ic0_forward, chunks, -1);
+    chain(ic0_backward, chunks, -1);
+    chain(ic0_start, blocks, -1);
     for (int k = 0; k < iters; ++k) {
-        chain(cg64_product<STORAGE>, blocks);
-        chain(ic0_update, blocks);
-        chain(ic0_forward, chunks);
-        chain(ic0_backward, chunks);
-        chain(ic0_dot, blocks);
-        chain(cg64_direction, blocks);
+        chain(cg64_product<STORAGE>, blocks, 0);
+        chain(ic0_update, blocks, 1);
+        chain(ic0_forward, chunks, 2);
+        chain(ic0_backward, chunks, 3);
+        chain(ic0_dot, blocks, 4);
+        chain(cg64_direction, blocks, 5);
     }
 }
 
@@ -1044,13 +1083,16 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         LF_REQUIRE(s.unrolled <= 100000, LFGPU_ERR_ARGUMENT, "profiling runs are limited to 100000 passes");
         const bool mx = s.mixed != 0;
         LF_CUDA(cudaEventRecord(c.ev_a, c.stream));
-        if (csr && jac) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled);
-        else if (csr) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled);
-        else if (jac) launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled);
-        else launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled);
+        EventTrail trail(c.stream, s.unrolled <= kTimedPasses);
+        if (csr && jac) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
+        else if (csr) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled, trail);
+        else if (jac) launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
+        else launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled, trail);
         LF_CUDA(cudaEventRecord(c.ev_b, c.stream));
         *kernel_ms = elapsed_ms(c);
-        return finish_cg(c, s);
+        PcgResult res = finish_cg(c, s);
+        trail.totals(res.phase_ns);
+        return res;
     }
     GraphBuilder gb{c};
     LF_CUDA(cudaGraphCreate(&gb.graph, 0));
@@ -1154,13 +1196,16 @@ PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double*
     LF_CUDA(cudaMemsetAsync(c.cg_state.p, 0, sizeof(CgState), c.stream));
     const bool csr = s.storage == LFGPU_STORAGE_CSR;
     a.use_cond = s.unrolled > 0 ? 0 : 1;
+    unsigned long long phase_ns[6] = {};
     if (s.unrolled > 0) {
         LF_REQUIRE(s.unrolled <= 100000, LFGPU_ERR_ARGUMENT, "profiling runs are limited to 100000 passes");
         LF_CUDA(cudaEventRecord(c.ev_a, c.stream));
-        if (csr) launch_ic0_unrolled<LFGPU_STORAGE_CSR>(c.stream, &a, blocks, chunks, s.unrolled);
-        else launch_ic0_unrolled<LFGPU_STORAGE_BSR>(c.stream, &a, blocks, chunks, s.unrolled);
+        EventTrail trail(c.stream, s.unrolled <= kTimedPasses);
+        if (csr) launch_ic0_unrolled<LFGPU_STORAGE_CSR>(c.stream, &a, blocks, chunks, s.unrolled, trail);
+        else launch_ic0_unrolled<LFGPU_STORAGE_BSR>(c.stream, &a, blocks, chunks, s.unrolled, trail);
         LF_CUDA(cudaEventRecord(c.ev_b, c.stream));
         *kernel_ms = elapsed_ms(c);
+        trail.totals(phase_ns);
     } else {
         GraphBuilder gb{c};
         LF_CUDA(cudaGraphCreate(&gb.graph, 0));
@@ -1177,6 +1222,7 @@ PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double*
         *kernel_ms = elapsed_ms(c);
     }
     PcgResult res = finish_cg(c, s);
+    for (int k = 0; k < 6; ++k) res.phase_ns[k] = phase_ns[k];
     // Time one standalone application (forward + backward sweep) on the final
     // residual; the solve made iterations + 1 of them.
     LF_CUDA(cudaEventRecord(c.ev_a, c.stream));

@@ -147,6 +147,7 @@ struct Context {
 
     // solve vectors and scratch
     Buf<double> u, R;
+    Buf<double> lam, adj_rhs;             // adjoint solution and right-hand side
     Buf<double> v64[6];
     Buf<float> v32[6];
     Buf<double> partials;                 // kSlots * kMaxReduce * max CTAs
