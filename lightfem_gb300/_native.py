@@ -266,10 +266,10 @@ class Context:
     @staticmethod
     def options(tolerance: float, max_iterations: int, storage: str = "csr", preconditioner: str = "jacobi",
                 precision: str = "fp64", refinement: str = "reliable", inner_reduction: float = 0.0,
-                max_refinements: int = 0, persistent: bool = False, unrolled: int = 0) -> SolveOptions:
+                max_refinements: int = 0, persistent: int = 0, unrolled: int = 0) -> SolveOptions:
         return SolveOptions(float(tolerance), int(max_iterations), STORAGE[storage], PRECOND[preconditioner],
                             PRECISION[precision], REFINEMENT[refinement], float(inner_reduction),
-                            int(max_refinements), int(bool(persistent)), int(unrolled))
+                            int(max_refinements), int(persistent), int(unrolled))
 
     def solve(self, options: SolveOptions, download: bool = True):
         rep = Report()

@@ -254,6 +254,9 @@ int lfgpu_destroy(lfgpu_t h) {
     h->status.release();
     h->pcg_result.release();
     h->ic0_misc.release();
+    for (auto& b : h->zp) b.release();
+    h->xhi.release();
+    h->xlo.release();
     for (auto& sc : h->sched) {
         sc.tiles.release();
         sc.cta.release();

@@ -21,6 +21,7 @@
 #include "common.cuh"
 #include "kernels.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -35,6 +36,10 @@ struct CgState {
     long long it, refs;
     int status, converged, stagnated, done, no_progress, refine;
     unsigned int count[4];
+    // FP32 copies for the mixed loop, set where alpha and beta are, so that no
+    // thread of the loop kernels converts them (GB300's FP64 pipe is narrow):
+    // alpha = alpha32 + alpha32_lo to about 48 bits.
+    float alpha32, alpha32_lo, beta32, pad32;
 };
 
 struct CgArgs {
@@ -62,10 +67,12 @@ struct CgArgs {
     double* q;
     double* r64;
     float* r32;
-    float* z32;
-    float* pa;
-    float* pb;
+    float* p32;
     float* q32;
+    float2* zp0;                   // (z, p) per DOF, two alternating copies
+    float2* zp1;
+    float* xhi;                    // FP32 pair of the solution correction
+    float* xlo;
     double* partials;  // 4 slots x blocks x 4
     const int* diag;               // IC(0): diagonal position of every row
     const double* icf;             // IC(0) factor on the pattern of K (ic0.cu)
@@ -92,16 +99,14 @@ __device__ __forceinline__ void set_branch(const CgArgs& a, bool go) {
 // Block sums of K values, then the last block to finish adds every block's sums in
 // block order and runs fin(totals) on thread 0.
 template <int K, typename Final>
-__device__ __forceinline__ void reduce_last(const CgArgs& a, int slot, double (&v)[K], Final&& fin) {
-    __shared__ double s_red[32 * kMaxReduce];
+__device__ __forceinline__ void reduce_tail(const CgArgs& a, int slot, double (&v)[K], double* s_red, Final&& fin) {
     __shared__ int s_last;
-    block_sum<K>(v, s_red);
     double* part = a.partials + static_cast<size_t>(slot) * a.blocks * kMaxReduce;
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int k = 0; k < K; ++k) part[blockIdx.x * kMaxReduce + k] = v[k];
-        __threadfence();
-        const unsigned t = atomicAdd(&a.st->count[slot], 1u);
+        unsigned t;  // arrive with release semantics: the partials above are visible first
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(t) : "l"(&a.st->count[slot]) : "memory");
         s_last = t == gridDim.x - 1;
     }
     __syncthreads();
@@ -119,6 +124,82 @@ __device__ __forceinline__ void reduce_last(const CgArgs& a, int slot, double (&
         a.st->count[slot] = 0;
         fin(acc);
     }
+}
+
+// FP64 per-thread values: FP64 warp and block sums.
+template <int K, typename Final>
+__device__ __forceinline__ void reduce_last(const CgArgs& a, int slot, double (&v)[K], Final&& fin) {
+    __shared__ double s_red[32 * kMaxReduce];
+    block_sum<K>(v, s_red);
+    reduce_tail<K>(a, slot, v, s_red, fin);
+}
+
+// An unevaluated FP32 pair (hi + lo) for the dot products of the FP32 loop: each
+// addition is Knuth's two-sum, so the pair carries about 48 bits.  This keeps
+// the dot products near FP64 accuracy with FP32 arithmetic only -- FP64 shuffles
+// and adds in every thread would keep GB300's narrow FP64 pipe busy for several
+// microseconds per reduction.
+struct FloatPair {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float s = __fadd_rn(hi, x);
+        const float bp = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+        lo = __fadd_rn(lo, e);
+        hi = s;
+    }
+    __device__ __forceinline__ void add(const FloatPair& o) {
+        add(o.hi);
+        lo = __fadd_rn(lo, o.lo);
+    }
+};
+
+// FP32-pair per-thread values (the mixed inner loop): warp sums as pairs, the
+// warps' sums added in FP64 by thread 0.
+template <int K, typename Final>
+__device__ __forceinline__ void reduce_last(const CgArgs& a, int slot, FloatPair (&v)[K], Final&& fin) {
+    __shared__ double s_red[32 * kMaxReduce];
+    __shared__ float2 s_warp[32 * kMaxReduce];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            FloatPair other;
+            other.hi = __shfl_xor_sync(0xffffffffu, v[k].hi, o);
+            other.lo = __shfl_xor_sync(0xffffffffu, v[k].lo, o);
+            v[k].add(other);
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) s_warp[warp * K + k] = make_float2(v[k].hi, v[k].lo);
+    }
+    __syncthreads();
+    double d[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) d[k] = 0.0;
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            FloatPair w;
+            if (lane < nw) {
+                const float2 t = s_warp[lane * K + k];
+                w.hi = t.x;
+                w.lo = t.y;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                FloatPair other;
+                other.hi = __shfl_xor_sync(0xffffffffu, w.hi, o);
+                other.lo = __shfl_xor_sync(0xffffffffu, w.lo, o);
+                w.add(other);
+            }
+            d[k] = static_cast<double>(w.hi) + static_cast<double>(w.lo);
+        }
+    }
+    reduce_tail<K>(a, slot, d, s_red, fin);
 }
 
 // Warp-uniform loop over row groups of 8 (quarter warp per row) across the grid.
@@ -195,22 +276,30 @@ __device__ __forceinline__ void bsr64_rows(const CgArgs& a, const G& g, Out&& ou
 }
 
 // FP32 BSR block rows, quarter warp per block row (one 16-byte block per lane).
+// Each lane keeps three blocks in flight (k, k+4, k+8), so the nine blocks of an
+// interior node's row cost one round of gather latency instead of three.
 template <typename G, typename Out>
 __device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& out) {
     rows_by_quad(a.nb, [&](bool act, int node, int sub) {
         float s0 = 0.f, s1 = 0.f;
         if (act) {
             const int b = __ldg(a.brow + node), e = __ldg(a.brow + node + 1);
-            for (int k = b + sub; k < e; k += 8) {  // two blocks in flight per lane
-                const bool two = k + 4 < e;
+            for (int k = b + sub; k < e; k += 12) {
+                const bool t1 = k + 4 < e, t2 = k + 8 < e;
+                const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+                const int c0 = ld_stream(a.bcol + k);
+                const int c1 = t1 ? ld_stream(a.bcol + k + 4) : c0;
+                const int c2 = t2 ? ld_stream(a.bcol + k + 8) : c0;
                 const float4 v0 = ld_stream(a.bval32 + k);
-                const float4 v1 = two ? ld_stream(a.bval32 + k + 4) : make_float4(0.f, 0.f, 0.f, 0.f);
-                const int c0 = ld_stream(a.bcol + k), c1 = two ? ld_stream(a.bcol + k + 4) : c0;
-                const float2 x0 = g(c0), x1 = g(c1);
+                const float4 v1 = t1 ? ld_stream(a.bval32 + k + 4) : zero;
+                const float4 v2 = t2 ? ld_stream(a.bval32 + k + 8) : zero;
+                const float2 x0 = g(c0), x1 = g(c1), x2 = g(c2);
                 s0 += v0.x * x0.x + v0.y * x0.y;
                 s1 += v0.z * x0.x + v0.w * x0.y;
                 s0 += v1.x * x1.x + v1.y * x1.y;
                 s1 += v1.z * x1.x + v1.w * x1.y;
+                s0 += v2.x * x2.x + v2.y * x2.y;
+                s1 += v2.z * x2.x + v2.w * x2.y;
             }
         }
         s0 = quad_sum(s0);
@@ -219,19 +308,28 @@ __device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& ou
     });
 }
 
+// FP32 CSR rows, quarter warp per row; five entries in flight per lane cover the
+// eighteen entries of an interior row in one round.
 template <typename G, typename Out>
 __device__ __forceinline__ void csr32_rows(const CgArgs& a, const G& g, Out&& out) {
     rows_by_quad(a.n, [&](bool act, int row, int sub) {
         float s = 0.f;
         if (act) {
             const int b = __ldg(a.rowptr + row), e = __ldg(a.rowptr + row + 1);
-            for (int k = b + sub; k < e; k += 8) {  // two independent units in flight per lane
-                const bool two = k + 4 < e;
-                const int c0 = ld_stream(a.col + k), c1 = two ? ld_stream(a.col + k + 4) : c0;
-                const float v0 = ld_stream(a.K32 + k), v1 = two ? ld_stream(a.K32 + k + 4) : 0.f;
-                const float x0 = g(c0), x1 = g(c1);
-                s += v0 * x0;
-                s += v1 * x1;
+            for (int k = b + sub; k < e; k += 20) {
+                int c[5];
+                float v[5];
+#pragma unroll
+                for (int j = 0; j < 5; ++j) {
+                    const bool on = k + 4 * j < e;
+                    c[j] = on ? ld_stream(a.col + k + 4 * j) : ld_stream(a.col + k);
+                    v[j] = on ? ld_stream(a.K32 + k + 4 * j) : 0.f;
+                }
+                float x[5];
+#pragma unroll
+                for (int j = 0; j < 5; ++j) x[j] = g(c[j]);
+#pragma unroll
+                for (int j = 0; j < 5; ++j) s += v[j] * x[j];
             }
         }
         s = quad_sum(s);
@@ -413,23 +511,49 @@ __global__ void __launch_bounds__(kThreads) cg64_direction(CgArgs a) {
 }
 
 // ------------------------------------------------------------------ mixed kernels
+// FP32 vectors of the inner solve.  z and p are interleaved per DOF, (z_c, p_c),
+// so the product gathers both with one 16-byte load per node; two copies
+// alternate between iterations (the product reads one, the update writes the
+// other).  The solution correction since the last residual replacement is kept
+// as an unevaluated FP32 pair (hi + lo, about 48 significant bits) and added to
+// the FP64 solution when a replacement is due, so no FP64 arithmetic runs per
+// iteration.
 __device__ __forceinline__ float pnew(float z, float p, float beta) { return __fmaf_rn(beta, p, z); }
 __device__ __forceinline__ float with_diag(float off, float hi, float lo, float x) { return fmaf(hi, x, off) + lo * x; }
+
+__device__ __forceinline__ float4* zp_buffer(const CgArgs& a, long long it) {
+    return reinterpret_cast<float4*>((it & 1) ? a.zp1 : a.zp0);
+}
+
+// (hi, lo) += (ah + al) * p with error-free transformations (Knuth's two-sum,
+// the fma two-product), then renormalised so |lo| <= ulp(hi) / 2.  The _rn
+// intrinsics keep the compiler from fusing the steps the error terms rely on.
+__device__ __forceinline__ void pair_axpy(float& hi, float& lo, float ah, float al, float p) {
+    const float prod = __fmul_rn(ah, p);
+    const float perr = __fmaf_rn(al, p, __fmaf_rn(ah, p, -prod));
+    const float s = __fadd_rn(hi, prod);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(prod, bp));
+    const float l = __fadd_rn(lo, __fadd_rn(err, perr));
+    hi = __fadd_rn(s, l);
+    lo = __fsub_rn(l, __fsub_rn(hi, s));
+}
 
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
     double v[2] = {0.0, 0.0};
     const double2* f2 = reinterpret_cast<const double2*>(a.f);
+    float4* zp = reinterpret_cast<float4*>(a.zp0);
     GRID_NODES(i) {
         const double2 fv = f2[i];
         const float2 rv = make_float2(static_cast<float>(fv.x), static_cast<float>(fv.y));
         const float2 zv = precond32<PRECOND>(a, i, rv);
         reinterpret_cast<double2*>(a.x)[i] = make_double2(0.0, 0.0);
+        reinterpret_cast<float2*>(a.xhi)[i] = make_float2(0.f, 0.f);
+        reinterpret_cast<float2*>(a.xlo)[i] = make_float2(0.f, 0.f);
         reinterpret_cast<double2*>(a.r64)[i] = fv;
         reinterpret_cast<float2*>(a.r32)[i] = rv;
-        reinterpret_cast<float2*>(a.z32)[i] = zv;
-        reinterpret_cast<float2*>(a.pa)[i] = make_float2(0.f, 0.f);
-        reinterpret_cast<float2*>(a.pb)[i] = make_float2(0.f, 0.f);
+        zp[i] = make_float4(zv.x, 0.f, zv.y, 0.f);
         v[0] += fv.x * fv.x + fv.y * fv.y;
         v[1] += static_cast<double>(rv.x * zv.x + rv.y * zv.y);
     }
@@ -438,6 +562,7 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
         s->r0 = s->rnorm = s->rmax = s->rtrue = s->rtrue_prev = sqrt(fmax(0.0, t[0]));
         s->rho = t[1];
         s->beta = 0.0;
+        s->beta32 = 0.f;
         s->it = 0;
         s->refs = 0;
         if (s->r0 <= a.target) {
@@ -455,41 +580,43 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
 template <int STORAGE>
 __global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
     if (a.st->done) return;
-    const float beta = static_cast<float>(a.st->beta);
-    const bool odd = a.st->it & 1;
-    const float* po = odd ? a.pb : a.pa;
-    float* pc = odd ? a.pa : a.pb;
-    float acc = 0.f;
+    const float beta = a.st->beta32;
+    const float4* zp4 = zp_buffer(a, a.st->it);
+    FloatPair acc;
     if (STORAGE == LFGPU_STORAGE_CSR) {
-        const float* z = a.z32;
-        csr32_rows(a, [&](int c) { return pnew(z[c], po[c], beta); }, [&](int row, float off) {
-            const float pn = pnew(z[row], po[row], beta);
-            const float y = with_diag(off, a.dhi[row], a.dlo[row], pn);
-            pc[row] = pn;
-            a.q32[row] = y;
-            acc += pn * y;
-        });
+        const float2* zp2 = reinterpret_cast<const float2*>(zp4);
+        csr32_rows(a,
+                   [&](int c) {
+                       const float2 v = zp2[c];
+                       return pnew(v.x, v.y, beta);
+                   },
+                   [&](int row, float off) {
+                       const float2 v = zp2[row];
+                       const float pn = pnew(v.x, v.y, beta);
+                       const float y = with_diag(off, a.dhi[row], a.dlo[row], pn);
+                       a.p32[row] = pn;
+                       a.q32[row] = y;
+                       acc.add(pn * y);
+                   });
     } else {
-        const float2* z2 = reinterpret_cast<const float2*>(a.z32);
-        const float2* po2 = reinterpret_cast<const float2*>(po);
         const float2* hi2 = reinterpret_cast<const float2*>(a.dhi);
         const float2* lo2 = reinterpret_cast<const float2*>(a.dlo);
         bsr32_rows(a,
                    [&](int c) {
-                       const float2 zv = z2[c], pv = po2[c];
-                       return make_float2(pnew(zv.x, pv.x, beta), pnew(zv.y, pv.y, beta));
+                       const float4 v = zp4[c];
+                       return make_float2(pnew(v.x, v.y, beta), pnew(v.z, v.w, beta));
                    },
                    [&](int node, float2 off) {
-                       const float2 zv = z2[node], pv = po2[node];
-                       const float2 pn = make_float2(pnew(zv.x, pv.x, beta), pnew(zv.y, pv.y, beta));
+                       const float4 v = zp4[node];
+                       const float2 pn = make_float2(pnew(v.x, v.y, beta), pnew(v.z, v.w, beta));
                        const float2 h = hi2[node], l = lo2[node];
                        const float2 y = make_float2(with_diag(off.x, h.x, l.x, pn.x), with_diag(off.y, h.y, l.y, pn.y));
-                       reinterpret_cast<float2*>(pc)[node] = pn;
+                       reinterpret_cast<float2*>(a.p32)[node] = pn;
                        reinterpret_cast<float2*>(a.q32)[node] = y;
-                       acc += pn.x * y.x + pn.y * y.y;
+                       acc.add(pn.x * y.x + pn.y * y.y);
                    });
     }
-    double v[1] = {acc};
+    FloatPair v[1] = {acc};
     reduce_last<1>(a, 1, v, [&](const double* t) {
         CgState* s = a.st;
         if (!(t[0] > 0.0) || !isfinite(t[0])) {
@@ -498,41 +625,44 @@ __global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
             set_loop(a, false);
         } else {
             s->alpha = s->rho / t[0];
+            s->alpha32 = static_cast<float>(s->alpha);
+            s->alpha32_lo = static_cast<float>(s->alpha - static_cast<double>(s->alpha32));
         }
     });
 }
 
+// x += alpha p (into the FP32 pair), r -= alpha q, z = M^-1 r; r.r and r.z.
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
     if (a.st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_branch(a, false);
         return;
     }
-    const double alpha64 = a.st->alpha;
-    const float alpha = static_cast<float>(alpha64);
-    const bool odd = a.st->it & 1;
-    const float2* pc2 = reinterpret_cast<const float2*>(odd ? a.pa : a.pb);
+    const float alpha = a.st->alpha32, alpha_lo = a.st->alpha32_lo;
+    const float2* p2 = reinterpret_cast<const float2*>(a.p32);
     const float2* q2 = reinterpret_cast<const float2*>(a.q32);
     float2* r2 = reinterpret_cast<float2*>(a.r32);
-    float2* z2 = reinterpret_cast<float2*>(a.z32);
-    double2* x2 = reinterpret_cast<double2*>(a.x);
-    float rr = 0.f, rz = 0.f;
+    float2* hi2 = reinterpret_cast<float2*>(a.xhi);
+    float2* lo2 = reinterpret_cast<float2*>(a.xlo);
+    float4* zp_next = zp_buffer(a, a.st->it + 1);
+    FloatPair rr, rz;
     GRID_NODES(i) {
-        const float2 pv = pc2[i], qv = q2[i];
-        double2 xv = x2[i];
+        const float2 pv = p2[i], qv = q2[i];
+        float2 hv = hi2[i], lv = lo2[i];
         float2 rv = r2[i];
-        xv.x += alpha64 * static_cast<double>(pv.x);
-        xv.y += alpha64 * static_cast<double>(pv.y);
+        pair_axpy(hv.x, lv.x, alpha, alpha_lo, pv.x);
+        pair_axpy(hv.y, lv.y, alpha, alpha_lo, pv.y);
         rv.x -= alpha * qv.x;
         rv.y -= alpha * qv.y;
         const float2 zv = precond32<PRECOND>(a, i, rv);
-        x2[i] = xv;
+        hi2[i] = hv;
+        lo2[i] = lv;
         r2[i] = rv;
-        z2[i] = zv;
-        rr += rv.x * rv.x + rv.y * rv.y;
-        rz += rv.x * zv.x + rv.y * zv.y;
+        zp_next[i] = make_float4(zv.x, pv.x, zv.y, pv.y);
+        rr.add(rv.x * rv.x + rv.y * rv.y);
+        rz.add(rv.x * zv.x + rv.y * zv.y);
     }
-    double v[2] = {rr, rz};
+    FloatPair v[2] = {rr, rz};
     reduce_last<2>(a, 2, v, [&](const double* t) {
         CgState* s = a.st;
         s->it += 1;
@@ -547,12 +677,32 @@ __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
                 s->done = 1;
             } else {
                 s->beta = t[1] / s->rho;
+                s->beta32 = static_cast<float>(s->beta);
                 s->rho = t[1];
             }
         }
         set_branch(a, refine && !s->done);
         set_loop(a, !s->done);
     });
+}
+
+// x64 += hi + lo, then hi = lo = 0 (hi + lo is exact in FP64).  Inside the loop it
+// runs only when a replacement is due; after the loop, always.
+template <bool ALWAYS>
+__global__ void __launch_bounds__(kThreads) mx_flush(CgArgs a) {
+    if (!ALWAYS && (a.st->done || !a.st->refine)) return;
+    double2* x2 = reinterpret_cast<double2*>(a.x);
+    float2* hi2 = reinterpret_cast<float2*>(a.xhi);
+    float2* lo2 = reinterpret_cast<float2*>(a.xlo);
+    GRID_NODES(i) {
+        const float2 hv = hi2[i], lv = lo2[i];
+        double2 xv = x2[i];
+        xv.x += static_cast<double>(hv.x) + static_cast<double>(lv.x);
+        xv.y += static_cast<double>(hv.y) + static_cast<double>(lv.y);
+        x2[i] = xv;
+        hi2[i] = make_float2(0.f, 0.f);
+        lo2[i] = make_float2(0.f, 0.f);
+    }
 }
 
 // FP64 residual replacement: r64 = f - K64 x, r32 = r64.
@@ -604,15 +754,18 @@ template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
     if (a.st->done || !a.st->refine) return;
     const float2* r2 = reinterpret_cast<const float2*>(a.r32);
-    float2* z2 = reinterpret_cast<float2*>(a.z32);
-    float rz = 0.f;
+    float4* zp = zp_buffer(a, a.st->it);  // the copy the next product reads
+    FloatPair rz;
     GRID_NODES(i) {
         const float2 rv = r2[i];
         const float2 zv = precond32<PRECOND>(a, i, rv);
-        z2[i] = zv;
-        rz += rv.x * zv.x + rv.y * zv.y;
+        float4 t = zp[i];
+        t.x = zv.x;
+        t.z = zv.y;
+        zp[i] = t;
+        rz.add(rv.x * zv.x + rv.y * zv.y);
     }
-    double v[1] = {rz};
+    FloatPair v[1] = {rz};
     reduce_last<1>(a, 2, v, [&](const double* t) {
         CgState* s = a.st;
         if (!(t[0] > 0.0) || !isfinite(t[0])) {
@@ -620,6 +773,7 @@ __global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
             s->done = 1;
         } else {
             s->beta = a.restart ? 0.0 : t[0] / s->rho;
+            s->beta32 = static_cast<float>(s->beta);
             s->rho = t[0];
         }
         set_loop(a, !s->done);
@@ -640,7 +794,7 @@ __global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
 // thread polls (bounded) until its operand appears: in shared memory when the
 // operand's row is in the same chunk, else in global memory at GPU scope.  Chunks
 // are taken in dependency order, so the oldest unfinished row can always proceed.
-constexpr int kSweepRows = kThreads;
+constexpr int kSweepRows = 256;
 constexpr unsigned long long kPending = ~0ull;  // a NaN pattern marking "not written yet"
 
 // A result that happens to carry the kPending pattern is stored as the default NaN.
@@ -853,12 +1007,12 @@ struct GraphBuilder {
 
 template <typename K>
 void add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep, int ndep, K kernel, int blocks,
-                CgArgs* args) {
+                CgArgs* args, int smem = 0, int threads = kThreads) {
     cudaKernelNodeParams p = {};
     p.func = reinterpret_cast<void*>(kernel);
     p.gridDim = dim3(blocks);
-    p.blockDim = dim3(kThreads);
-    p.sharedMemBytes = 0;
+    p.blockDim = dim3(threads);
+    p.sharedMemBytes = smem;
     void* params[1] = {args};
     p.kernelParams = params;
     LF_CUDA(cudaGraphAddKernelNode(node, g, dep, ndep, &p));
@@ -896,16 +1050,19 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks) {
     cudaGraphNode_t n_init;
     add_kernel(g, &n_init, nullptr, 0, mx_init<PRECOND>, blocks, a);
     cudaGraph_t body;
-    add_conditional(g, &n_init, 1, a->loop, cudaGraphCondTypeWhile, &body);
+    const cudaGraphNode_t n_loop = add_conditional(g, &n_init, 1, a->loop, cudaGraphCondTypeWhile, &body);
+    cudaGraphNode_t n_flush;
+    add_kernel(g, &n_flush, &n_loop, 1, mx_flush<true>, blocks, a);
     // The IF node lives in the loop body, so its handle belongs to that graph.
     LF_CUDA(cudaGraphConditionalHandleCreate(&a->branch, body, 0, 0));
-    cudaGraphNode_t k1, k2, k3, k4;
+    cudaGraphNode_t k1, k2, k3, k4, k5;
     add_kernel(body, &k1, nullptr, 0, mx_product<STORAGE>, blocks, a);
     add_kernel(body, &k2, &k1, 1, mx_update<PRECOND>, blocks, a);
     cudaGraph_t branch;
     add_conditional(body, &k2, 1, a->branch, cudaGraphCondTypeIf, &branch);
-    add_kernel(branch, &k3, nullptr, 0, mx_residual<STORAGE>, blocks, a);
-    add_kernel(branch, &k4, &k3, 1, mx_reprecondition<PRECOND>, blocks, a);
+    add_kernel(branch, &k3, nullptr, 0, mx_flush<false>, blocks, a);
+    add_kernel(branch, &k4, &k3, 1, mx_residual<STORAGE>, blocks, a);
+    add_kernel(branch, &k5, &k4, 1, mx_reprecondition<PRECOND>, blocks, a);
 }
 
 // Per-kernel device time of the profiling form: an event after every launch; the
@@ -958,6 +1115,7 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
         if (mixed) {
             chain(mx_product<STORAGE>, 0);
             chain(mx_update<PRECOND>, 1);
+            chain(mx_flush<false>, 2);
             chain(mx_residual<STORAGE>, 2);
             chain(mx_reprecondition<PRECOND>, 3);
         } else {
@@ -966,6 +1124,7 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
             chain(cg64_direction, 2);
         }
     }
+    if (mixed) chain(mx_flush<true>, -1);
 }
 
 // IC(0): init -> forward -> backward -> start -> WHILE { product ; update ;
@@ -975,16 +1134,16 @@ void build_ic0(cudaGraph_t g, CgArgs* a, int blocks, int chunks) {
     cudaGraphNode_t n_res = nullptr, n_init, n_fwd, n_bwd, n_start;
     if (a->x0) add_kernel(g, &n_res, nullptr, 0, cg64_residual<STORAGE>, blocks, a);
     add_kernel(g, &n_init, a->x0 ? &n_res : nullptr, a->x0 ? 1 : 0, ic0_init, blocks, a);
-    add_kernel(g, &n_fwd, &n_init, 1, ic0_forward, chunks, a);
-    add_kernel(g, &n_bwd, &n_fwd, 1, ic0_backward, chunks, a);
+    add_kernel(g, &n_fwd, &n_init, 1, ic0_forward, chunks, a, 0, kSweepRows);
+    add_kernel(g, &n_bwd, &n_fwd, 1, ic0_backward, chunks, a, 0, kSweepRows);
     add_kernel(g, &n_start, &n_bwd, 1, ic0_start, blocks, a);
     cudaGraph_t body;
     add_conditional(g, &n_start, 1, a->loop, cudaGraphCondTypeWhile, &body);
     cudaGraphNode_t k[6];
     add_kernel(body, &k[0], nullptr, 0, cg64_product<STORAGE>, blocks, a);
     add_kernel(body, &k[1], &k[0], 1, ic0_update, blocks, a);
-    add_kernel(body, &k[2], &k[1], 1, ic0_forward, chunks, a);
-    add_kernel(body, &k[3], &k[2], 1, ic0_backward, chunks, a);
+    add_kernel(body, &k[2], &k[1], 1, ic0_forward, chunks, a, 0, kSweepRows);
+    add_kernel(body, &k[3], &k[2], 1, ic0_backward, chunks, a, 0, kSweepRows);
     add_kernel(body, &k[4], &k[3], 1, ic0_dot, blocks, a);
     add_kernel(body, &k[5], &k[4], 1, cg64_direction, blocks, a);
 }
@@ -993,23 +1152,28 @@ void build_ic0(cudaGraph_t g, CgArgs* a, int blocks, int chunks) {
 // 5 p update.
 template <int STORAGE>
 void launch_ic0_unrolled(cudaStream_t stream, CgArgs* a, int blocks, int chunks, int iters, EventTrail& trail) {
-    auto chain = [&](auto kernel, int grid, int phase) {
-        kernel<<<grid, kThreads, 0, stream>>>(*a);
+    auto chain = [&](auto kernel, int phase) {  // the loop kernels
+        kernel<<<blocks, kThreads, 0, stream>>>(*a);
         LF_CUDA(cudaGetLastError());
         trail.mark(phase);
     };
-    if (a->x0) chain(cg64_residual<STORAGE>, blocks, -1);
-    chain(ic0_init, blocks, -1);
-    chain(ic0_forward, chunks, -1);
-    chain(ic0_backward, chunks, -1);
-    chain(ic0_start, blocks, -1);
+    auto sweep = [&](auto kernel, int phase) {  // one CTA of kSweepRows threads per row chunk
+        kernel<<<chunks, kSweepRows, 0, stream>>>(*a);
+        LF_CUDA(cudaGetLastError());
+        trail.mark(phase);
+    };
+    if (a->x0) chain(cg64_residual<STORAGE>, -1);
+    chain(ic0_init, -1);
+    sweep(ic0_forward, -1);
+    sweep(ic0_backward, -1);
+    chain(ic0_start, -1);
     for (int k = 0; k < iters; ++k) {
-        chain(cg64_product<STORAGE>, blocks, 0);
-        chain(ic0_update, blocks, 1);
-        chain(ic0_forward, chunks, 2);
-        chain(ic0_backward, chunks, 3);
-        chain(ic0_dot, blocks, 4);
-        chain(cg64_direction, blocks, 5);
+        chain(cg64_product<STORAGE>, 0);
+        chain(ic0_update, 1);
+        sweep(ic0_forward, 2);
+        sweep(ic0_backward, 3);
+        chain(ic0_dot, 4);
+        chain(cg64_direction, 5);
     }
 }
 
@@ -1049,10 +1213,15 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
     if (s.mixed) {
         for (auto& b : c.v32) b.ensure(n);
         a.r32 = c.v32[0];
-        a.z32 = c.v32[1];
-        a.pa = c.v32[2];
-        a.pb = c.v32[3];
+        a.p32 = c.v32[2];
         a.q32 = c.v32[4];
+        for (auto& b : c.zp) b.ensure(n);
+        a.zp0 = c.zp[0];
+        a.zp1 = c.zp[1];
+        c.xhi.ensure(n);
+        c.xlo.ensure(n);
+        a.xhi = c.xhi;
+        a.xlo = c.xlo;
         if (s.storage == LFGPU_STORAGE_BSR) {
             ensure_bsr32(c);
             a.bval32 = reinterpret_cast<const float4*>(c.bval32.p);
@@ -1131,9 +1300,10 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     if (s.precond == LFGPU_PRECOND_IC0)
         c.launches += (s.x0 ? 1 : 0) + 4 + 6 * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
     else if (s.unrolled > 0)
-        c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 4 : 3);
-    else
-        c.launches += (s.x0 ? 1 : 0) + 1 + (s.mixed ? 2 * st.it + 2 * st.refs : 3 * st.it);
+        c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 5 : 3) +
+                      (s.mixed ? 1 : 0);
+    else  // mixed: the branch runs flush, residual and re-preconditioning; a final flush follows the loop
+        c.launches += (s.x0 ? 1 : 0) + 1 + (s.mixed ? 2 * st.it + 3 * st.refs + 1 : 3 * st.it);
     PcgResult r{};
     r.iterations = st.it;
     r.refinements = st.refs;

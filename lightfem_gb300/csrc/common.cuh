@@ -148,6 +148,8 @@ struct Context {
     // solve vectors and scratch
     Buf<double> u, R;
     Buf<double> lam, adj_rhs;             // adjoint solution and right-hand side
+    Buf<float2> zp[2];                    // mixed graph loop: (z, p) per DOF, two copies
+    Buf<float> xhi, xlo;                  // mixed graph loop: FP32 pair of the solution correction
     Buf<double> v64[6];
     Buf<float> v32[6];
     Buf<double> partials;                 // kSlots * kMaxReduce * max CTAs
