@@ -370,20 +370,23 @@ def run_ours(args) -> int:
     main = opts("mixed")
     if args.profile_iters:
         # Profiling run (not a benchmark): one step with the PCG capped at
-        # --profile-iters iterations, then three standalone products of each kind.
-        capped = ctx.options(tol, args.profile_iters, args.storage, args.precond, "mixed", "reliable")
+        # --profile-iters iterations, the same loop with its kernels launched on the
+        # stream, then three standalone products of each kind.  IC(0) runs in FP64.
+        precision = "fp64" if args.precond == "ic0" else "mixed"
+        capped = ctx.options(tol, args.profile_iters, args.storage, args.precond, precision, "reliable")
         ms, rep = step(capped)
-        unrolled = ctx.options(tol, 10 ** 6, args.storage, args.precond, "mixed", "reliable",
+        unrolled = ctx.options(tol, 10 ** 6, args.storage, args.precond, precision, "reliable",
                                unrolled=args.profile_iters)
         ms_u, rep_u = step(unrolled)
         x = np.random.default_rng(0).standard_normal(n)
         for st in ("csr", "bsr"):
             for prec in ("fp64", "mixed"):
                 ctx.spmv(x, 1, st, prec, repeat=3)
-        print(json.dumps({"profile_iters": args.profile_iters, "conditional_step_ms": ms,
-                          "conditional_solve_ms": rep.solve_ms, "iterations": rep.iterations,
-                          "unrolled_step_ms": ms_u, "unrolled_solve_ms": rep_u.solve_ms,
-                          "unrolled_iterations": rep_u.iterations}))
+        print(json.dumps({"profile_iters": args.profile_iters, "precision": precision,
+                          "conditional_step_ms": ms, "conditional_solve_ms": rep.solve_ms,
+                          "iterations": rep.iterations, "unrolled_step_ms": ms_u,
+                          "unrolled_solve_ms": rep_u.solve_ms, "unrolled_iterations": rep_u.iterations,
+                          "unrolled_kernel_ms": list(rep_u.phase_ms)}))
         ctx.close()
         return 0
     for _ in range(args.warmup):
@@ -543,7 +546,8 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--storage", choices=("csr", "bsr"), default="bsr")
-    ap.add_argument("--precond", choices=("jacobi", "block"), default="jacobi")
+    ap.add_argument("--precond", choices=("jacobi", "block", "ic0"), default="jacobi",
+                    help="ic0 only with --profile-iters (FP64 profiling run)")
     ap.add_argument("--scale", type=int, default=1, help="divide the mesh size (testing only)")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -556,6 +560,8 @@ def main() -> int:
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling run for ncu: one step capped at this many PCG iterations (not a benchmark)")
     args = ap.parse_args()
+    if args.precond == "ic0" and not args.profile_iters:
+        ap.error("--precond ic0 is a profiling option (use it with --profile-iters)")
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")
     return run_reference(args) if args.impl == "reference" else run_ours(args)
