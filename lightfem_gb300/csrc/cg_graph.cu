@@ -794,7 +794,7 @@ __global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
 // thread polls (bounded) until its operand appears: in shared memory when the
 // operand's row is in the same chunk, else in global memory at GPU scope.  Chunks
 // are taken in dependency order, so the oldest unfinished row can always proceed.
-constexpr int kSweepRows = 256;
+constexpr int kSweepRows = 1024;  // rows per chunk, one CTA thread per row
 constexpr unsigned long long kPending = ~0ull;  // a NaN pattern marking "not written yet"
 
 // A result that happens to carry the kPending pattern is stored as the default NaN.
@@ -820,12 +820,22 @@ __device__ __forceinline__ double poll_shared(const volatile unsigned long long*
     unsigned long long v = *p;
     if (v == kPending) {
         const unsigned long long t0 = global_ns();
-        for (unsigned it = 1; (v = *p) == kPending; ++it)
+        for (unsigned it = 1; (v = *p) == kPending; ++it) {
+            // Back off: the producer of the operand is often a lane of this same
+            // warp, which only runs while this lane's path yields.
+            __nanosleep(32);
             if ((it & 1023u) == 0u && wait_expired(status, t0, row)) break;
+        }
     }
     return __longlong_as_double(static_cast<long long>(v));
 }
 
+// One CTA per chunk of kSweepRows consecutive rows.  The critical path of a sweep
+// crosses chunks only at some of its levels: inside a chunk an operand is a
+// shared-memory poll away, across chunks an L2 round trip, so larger chunks
+// shorten the path (1024 rows: 14 % faster than 256 on the 200x200 workload).
+// Giving a thread several rows of a chunk, in order, is much slower: a row then
+// also waits for the thread's earlier rows, which can sit many levels later.
 __global__ void __launch_bounds__(kSweepRows) ic0_forward(CgArgs a) {
     if (a.st->done) return;
     __shared__ unsigned long long s_v[kSweepRows];
@@ -1157,7 +1167,7 @@ void launch_ic0_unrolled(cudaStream_t stream, CgArgs* a, int blocks, int chunks,
         LF_CUDA(cudaGetLastError());
         trail.mark(phase);
     };
-    auto sweep = [&](auto kernel, int phase) {  // one CTA of kSweepRows threads per row chunk
+    auto sweep = [&](auto kernel, int phase) {  // one CTA per chunk of kSweepRows rows
         kernel<<<chunks, kSweepRows, 0, stream>>>(*a);
         LF_CUDA(cudaGetLastError());
         trail.mark(phase);
