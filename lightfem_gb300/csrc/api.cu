@@ -2,8 +2,11 @@
 // every index that reaches a kernel, uploads, and the orchestration of the solve
 // path stages on the handle's stream.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <thread>
 #include <cstring>
+#include <exception>
 #include <new>
 #include <string>
 #include <vector>
@@ -89,6 +92,9 @@ int guarded(lfgpu_t h, F&& f) {
     }
 }
 
+void install_colors(Context& c, const int* colors);
+void install_finish(Context& c);
+
 // Host copies the map/colour validation needs; set on lfgpu_set_pattern.
 void install_pattern(Context& c, i64 n, i64 nnz, const int64_t* rowptr64, const int* col, const int* map,
                      const int* colors) {
@@ -135,7 +141,20 @@ void install_pattern(Context& c, i64 n, i64 nnz, const int64_t* rowptr64, const 
             }
         }
     }
-    // Colours: per-colour element lists; no two elements of a colour may share a node.
+    install_colors(c, colors);
+    c.n = n;
+    c.nnz = nnz;
+    c.paired = paired;
+    upload(c, c.rowptr, rp.data(), rp.size());
+    upload(c, c.col, col, static_cast<size_t>(nnz));
+    upload(c, c.map, map, static_cast<size_t>(c.n_elem) * 64);
+    c.h_rowptr_cache = rp;
+    install_finish(c);
+}
+
+// Colours: per-colour element lists; no two elements of a colour may share a node.
+void install_colors(Context& c, const int* colors) {
+    const int* en = c.h_elem_nodes.data();
     c.n_colors = 0;
     c.color_offsets.assign(1, 0);
     std::vector<int> order;
@@ -165,13 +184,13 @@ void install_pattern(Context& c, i64 n, i64 nnz, const int64_t* rowptr64, const 
     } else {
         c.h_colors.clear();
     }
-    c.n = n;
-    c.nnz = nnz;
-    c.paired = paired;
-    upload(c, c.rowptr, rp.data(), rp.size());
-    upload(c, c.col, col, static_cast<size_t>(nnz));
-    upload(c, c.map, map, static_cast<size_t>(c.n_elem) * 64);
     upload(c, c.color_elems, order.data(), order.size());
+}
+
+// Device state that follows a new pattern (rowptr, col, map, n, nnz, paired and
+// the host row-pointer copy are in place).
+void install_finish(Context& c) {
+    const i64 n = c.n, nnz = c.nnz;
     c.diag.ensure(static_cast<size_t>(n));
     launch_find_diagonal(c);
     c.K.ensure(nnz);
@@ -187,7 +206,6 @@ void install_pattern(Context& c, i64 n, i64 nnz, const int64_t* rowptr64, const 
         LF_CUDA(cudaMemsetAsync(c.fixed.p, 0, n, c.stream));
         LF_CUDA(cudaMemsetAsync(c.prescribed.p, 0, sizeof(double) * n, c.stream));
     }
-    c.h_rowptr_cache = rp;
     c.h_brow.clear();
     c.have_pattern = true;
     c.assembled = c.constrained = c.solved = false;
@@ -327,13 +345,37 @@ int lfgpu_set_pattern(lfgpu_t h, int64_t n_dofs, int64_t nnz, const int64_t* row
 int lfgpu_build_pattern(lfgpu_t h) {
     return guarded(h, [&] {
         LF_REQUIRE(h->n_nodes > 0, LFGPU_ERR_STATE, "set the mesh before building the pattern");
-        LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
-        const HostPattern p = build_pattern(h->n_nodes, h->n_elem, h->h_elem_nodes.data());
+        const auto t0 = std::chrono::steady_clock::now();
+        // The greedy colouring is sequential in element order; it runs on a host
+        // thread while the device builds the pattern and the map.
         std::vector<int> colors;
-        greedy_colors(h->n_nodes, h->n_elem, h->h_elem_nodes.data(), colors);
-        install_pattern(*h, p.n, p.nnz, p.rowptr.data(), p.col.data(), p.map.data(), colors.data());
-        LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
-        h->timings.pattern_ms = elapsed_ms(*h);
+        std::exception_ptr colouring_error;
+        std::thread colouring([&] {
+            try {
+                greedy_colors(h->n_nodes, h->n_elem, h->h_elem_nodes.data(), colors);
+            } catch (...) {
+                colouring_error = std::current_exception();
+            }
+        });
+        bool on_device = false;
+        try {
+            on_device = build_pattern_device(*h, h->h_rowptr_cache);
+        } catch (...) {
+            colouring.join();
+            throw;
+        }
+        colouring.join();
+        if (colouring_error) std::rethrow_exception(colouring_error);
+        if (on_device) {
+            install_colors(*h, colors.data());
+            install_finish(*h);
+        } else {  // a node with more elements than the device build handles
+            const HostPattern p = build_pattern(h->n_nodes, h->n_elem, h->h_elem_nodes.data());
+            install_pattern(*h, p.n, p.nnz, p.rowptr.data(), p.col.data(), p.map.data(), colors.data());
+        }
+        h->pattern_on_device = on_device;
+        h->timings.pattern_ms =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     });
 }
 

@@ -103,6 +103,7 @@ struct Context {
     i64 n = 0, nnz = 0;
     bool have_pattern = false;
     bool paired = false;  // every row has even length and starts at an even offset with (2j, 2j+1) column pairs
+    bool pattern_on_device = false;  // lfgpu_build_pattern used the device build
     Buf<int> rowptr, col, map, diag;
     std::vector<int> h_rowptr_cache;
     std::vector<int> h_colors;

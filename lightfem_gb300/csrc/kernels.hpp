@@ -60,6 +60,10 @@ enum Ic0Slot {
 };
 void ensure_ic0(Context& c);
 
+// pattern.cu: CSR pattern and element->value map on the device; false if a node
+// has more elements than the device build handles (the caller builds on the host)
+bool build_pattern_device(Context& c, std::vector<int>& rowptr_host);
+
 // adjoint.cu
 void launch_adjoint_grad(Context& c, const double* u, const double* lam, double* grad);
 

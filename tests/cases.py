@@ -55,6 +55,24 @@ def adjoint_model() -> Model:
                            settings=SolverSettings(tolerance=1e-13, max_iterations=50000))
 
 
+def fan(sectors: int = 20) -> Model:
+    """Kite-shaped quads around one centre node, which belongs to every element (more
+    elements at one node than the device pattern build takes), plus an isolated
+    node that belongs to no element.  Node IDs are scrambled."""
+    theta = 2.0 * np.pi * np.arange(sectors) / sectors
+    mid = theta + np.pi / sectors
+    xy = np.vstack([[0.0, 0.0], np.c_[np.cos(theta), np.sin(theta)], 2.0 * np.c_[np.cos(mid), np.sin(mid)],
+                    [5.0, 5.0]])
+    ids = np.random.default_rng(3).permutation(xy.shape[0]) + 100
+    ring = lambda i: ids[1 + (i % sectors)]
+    outer = lambda i: ids[1 + sectors + i]
+    conn = np.array([[ids[0], ring(i), outer(i), ring(i + 1)] for i in range(sectors)])
+    return Model(node_ids=ids, xy=xy, material_ids=np.array([1]), young=np.array([1.0e6]),
+                 poisson=np.array([0.25]), thickness=np.array([1.0]), element_ids=np.arange(1, sectors + 1),
+                 element_nodes=conn, element_material=np.ones(sectors, np.int64),
+                 settings=SolverSettings(tolerance=1e-12, max_iterations=1000))
+
+
 CASES = {"single_q4": single_q4, "scrambled": scrambled, "grid6": grid6, "beam": beam, "strain": strain}
 
 # (storage, preconditioner, subdomain_split, subdomain_nodes) of each golden variant

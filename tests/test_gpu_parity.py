@@ -45,6 +45,29 @@ def test_pattern_map_colors_bit_exact(native, name):
     np.testing.assert_array_equal(colors, g["colors"])
 
 
+@pytest.mark.parametrize("build", ["grid", "fan"])
+def test_pattern_builds_match_oracle(native, oracle, build):
+    """The device pattern build (structured grids) and the host build it falls back
+    to (a node in more elements than the device build takes, an isolated node) both
+    equal the oracle's pattern, map and colours bit for bit."""
+    from cases import fan
+    if build == "fan":
+        model = fan()
+    else:  # a structured grid plus one node in no element
+        model = mesh.workload(1, scale=4)
+        model.node_ids = np.append(model.node_ids, model.node_ids.max() + 1)
+        model.xy = np.vstack([model.xy, [9.0, 9.0]])
+    model = indexed(model)
+    ctx = native.Context(0)
+    upload_model(ctx, model)
+    rp, col, mp, colors = ctx.download_pattern()
+    want_rp, want_col, want_map = oracle.pattern(model.n_dofs, model.element_dofs())
+    np.testing.assert_array_equal(rp, want_rp)
+    np.testing.assert_array_equal(col, want_col)
+    np.testing.assert_array_equal(mp, want_map)
+    np.testing.assert_array_equal(colors, oracle.colors(model.n_nodes, model.element_node_index()))
+
+
 @pytest.mark.parametrize("strategy", ["coloring", "atomic"])
 @pytest.mark.parametrize("name", list(CASES))
 def test_assembly_and_dirichlet(native, name, strategy):
