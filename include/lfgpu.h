@@ -25,6 +25,8 @@
  *         src/precond.cpp:298-412)
  *   lfgpu_reactions
  *        reaction = K_full u - f                           src/solver.cpp:953-954
+ *   lfgpu_postprocess
+ *        postprocess + smooth_nodal_stresses               src/solver.cpp:756-871
  *
  * Error mapping to the reference's exceptions (src/main.cpp:162-164 maps all of them
  * to exit code 4): LFGPU_ERR_JACOBIAN -> "Q4 stiffness evaluation received a
@@ -138,6 +140,7 @@ typedef struct lfgpu_timings {
     double reactions_ms;
     int64_t coloring_count;  /* colours used by the colouring strategy */
     int64_t kernel_launches; /* kernels this handle has launched so far (graph nodes included) */
+    double postprocess_ms;   /* element fields + nodal smoothing (lfgpu_postprocess) */
 } lfgpu_timings;
 
 /* --- handle ------------------------------------------------------------------- */
@@ -195,6 +198,15 @@ int lfgpu_apply_dirichlet(lfgpu_t h);
 int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* options, double* u_out, lfgpu_report* report);
 /* R = K_full u - f_full for the last solution; r_out may be NULL. */
 int lfgpu_reactions(lfgpu_t h, double* r_out);
+
+/* Post-processing of the last solution: postprocess + smooth_nodal_stresses
+ * (src/solver.cpp:756-871, q4_center_field / q4_gauss_point_fields
+ * src/element.cpp:212-248).  element_fields[35 e + 7 k + j] (may be NULL): k = 0
+ * the element centre, k = 1..4 the Gauss points (-g,-g), (g,-g), (g,g), (-g,g);
+ * j = strain xx, yy, xy, stress xx, yy, xy, von Mises.  nodal_stress[4 i + j]
+ * (may be NULL): smoothed stress xx, yy, xy and its von Mises, zero for a node in
+ * no element. */
+int lfgpu_postprocess(lfgpu_t h, double* element_fields, double* nodal_stress);
 int lfgpu_download(lfgpu_t h, int32_t which, double* out);
 int lfgpu_timings_get(lfgpu_t h, lfgpu_timings* out);
 

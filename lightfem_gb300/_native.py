@@ -54,7 +54,8 @@ class Report(ctypes.Structure):
 
 class Timings(ctypes.Structure):
     _fields_ = [("pattern_ms", c_double), ("assembly_ms", c_double), ("boundary_ms", c_double),
-                ("reactions_ms", c_double), ("coloring_count", c_int64), ("kernel_launches", c_int64)]
+                ("reactions_ms", c_double), ("coloring_count", c_int64), ("kernel_launches", c_int64),
+                ("postprocess_ms", c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -95,6 +96,7 @@ _SIGNATURES = {
     "lfgpu_event_elapsed": (c_int, [c_void_p, c_int32, c_int32, POINTER(c_double)]),
     "lfgpu_spmv": (c_int, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, POINTER(c_double)]),
     "lfgpu_adjoint": (c_int, [c_void_p, c_void_p, POINTER(SolveOptions), c_void_p, POINTER(Report)]),
+    "lfgpu_postprocess": (c_int, [c_void_p, c_void_p, c_void_p]),
     "lfgpu_apply_preconditioner": (c_int, [c_void_p, c_int32, c_void_p, c_void_p, POINTER(c_double)]),
     "lfgpu_residual_norm_noalloc": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                             POINTER(c_double)]),
@@ -314,6 +316,14 @@ class Context:
         self._check(self._lib.lfgpu_spmv(self._h, which, STORAGE[storage], PRECISION[precision], _ptr(x), _ptr(y),
                                          int(repeat), ctypes.byref(ms)))
         return y, ms.value
+
+    def postprocess(self):
+        """Element fields (E x 5 x 7: centre + 4 Gauss points; strain xx, yy, xy,
+        stress xx, yy, xy, von Mises) and smoothed nodal stress (N x 4)."""
+        fields = np.empty((self.n_elements, 5, 7))
+        nodal = np.empty((self.n_dofs // 2, 4))
+        self._check(self._lib.lfgpu_postprocess(self._h, _ptr(fields), _ptr(nodal)))
+        return fields, nodal
 
     def apply_preconditioner(self, r, preconditioner: str = "jacobi"):
         """z = M^-1 r for the constrained K; returns (z, device ms)."""

@@ -272,6 +272,10 @@ int lfgpu_destroy(lfgpu_t h) {
     h->status.release();
     h->pcg_result.release();
     h->ic0_misc.release();
+    h->ne_ptr.release();
+    h->ne_list.release();
+    h->post_fields.release();
+    h->post_nodal.release();
     for (auto& b : h->zp) b.release();
     h->xhi.release();
     h->xlo.release();
@@ -320,6 +324,7 @@ int lfgpu_set_mesh(lfgpu_t h, int64_t n_nodes, const double* xy, int64_t n_eleme
         upload(*h, h->mat_t, thickness, static_cast<size_t>(n_materials));
         h->h_elem_nodes.assign(element_nodes, element_nodes + 4 * n_elements);
         h->have_pattern = h->assembled = h->constrained = h->solved = false;
+        ++h->mesh_version;
         h->have_nodal = h->have_body = h->have_edges = false;
         h->n_constraints = 0;
         LF_CUDA(cudaStreamSynchronize(h->stream));
@@ -783,6 +788,26 @@ int lfgpu_spmv(lfgpu_t h, int32_t which, int32_t storage, int32_t precision, con
             }
         }
         check_status(*h);
+    });
+}
+
+int lfgpu_postprocess(lfgpu_t h, double* element_fields, double* nodal_stress) {
+    return guarded(h, [&] {
+        LF_REQUIRE(h->solved, LFGPU_ERR_STATE, "solve before post-processing");
+        h->post_fields.ensure(35 * static_cast<size_t>(h->n_elem) + 1);
+        h->post_nodal.ensure(4 * static_cast<size_t>(h->n_nodes));
+        LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
+        launch_postprocess(*h, h->u, h->post_fields, h->post_nodal);
+        LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
+        h->timings.postprocess_ms = elapsed_ms(*h);
+        check_status(*h);
+        if (element_fields)
+            LF_CUDA(cudaMemcpyAsync(element_fields, h->post_fields.p, sizeof(double) * 35 * h->n_elem,
+                                    cudaMemcpyDeviceToHost, h->stream));
+        if (nodal_stress)
+            LF_CUDA(cudaMemcpyAsync(nodal_stress, h->post_nodal.p, sizeof(double) * 4 * h->n_nodes,
+                                    cudaMemcpyDeviceToHost, h->stream));
+        LF_CUDA(cudaStreamSynchronize(h->stream));
     });
 }
 

@@ -98,6 +98,10 @@ struct Context {
     Buf<int> elem_mat;
     Buf<double> mat_young, mat_nu, mat_t;
     std::vector<int> h_elem_nodes;  // host copy for setup work
+    unsigned long long mesh_version = 0;  // bumps on lfgpu_set_mesh
+    Buf<int> ne_ptr, ne_list;             // node -> elements, ascending per node (post-processing)
+    unsigned long long ne_version = ~0ull;
+    Buf<double> post_fields, post_nodal;
 
     // pattern
     i64 n = 0, nnz = 0;

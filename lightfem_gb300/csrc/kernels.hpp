@@ -63,6 +63,11 @@ void ensure_ic0(Context& c);
 // pattern.cu: CSR pattern and element->value map on the device; false if a node
 // has more elements than the device build handles (the caller builds on the host)
 bool build_pattern_device(Context& c, std::vector<int>& rowptr_host);
+// node -> elements lists in ascending element order, cached per mesh (c.ne_ptr, c.ne_list)
+void ensure_node_elements(Context& c);
+
+// postprocess.cu: element fields (35 per element) and smoothed nodal stress (4 per node)
+void launch_postprocess(Context& c, const double* u, double* fields, double* nodal);
 
 // adjoint.cu
 void launch_adjoint_grad(Context& c, const double* u, const double* lam, double* grad);

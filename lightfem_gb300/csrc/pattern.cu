@@ -197,6 +197,23 @@ __global__ void fill_map(int ne, const int4* __restrict__ en, const int* __restr
     }
 }
 
+// Each node's element list in ascending element order (insertion sort: a node has
+// a handful of elements).
+__global__ void sort_node_elems(int nn, const int* __restrict__ nptr, int* list) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
+        const int b = nptr[i], e = nptr[i + 1];
+        for (int k = b + 1; k < e; ++k) {
+            const int v = list[k];
+            int p = k;
+            while (p > b && list[p - 1] > v) {
+                list[p] = list[p - 1];
+                --p;
+            }
+            list[p] = v;
+        }
+    }
+}
+
 // Exclusive scan of n ints on the stream; returns the total (synchronises).
 long long exclusive_scan(Context& c, const int* in, int* out, int n, Buf<long long>& tmp) {
     const int nb = (n + kScanBlock - 1) / kScanBlock;
@@ -213,6 +230,27 @@ long long exclusive_scan(Context& c, const int* in, int* out, int n, Buf<long lo
 }
 
 }  // namespace
+
+void ensure_node_elements(Context& c) {
+    if (c.ne_version == c.mesh_version) return;
+    const int nn = static_cast<int>(c.n_nodes), ne = static_cast<int>(c.n_elem);
+    const int grid_e = grid_for(ne, kThreads, 16 * c.num_sms), grid_n = grid_for(nn, kThreads, 16 * c.num_sms);
+    Buf<int> cnt, fill;
+    Buf<long long> tmp;
+    cnt.ensure(static_cast<size_t>(nn) + 1);
+    fill.ensure(static_cast<size_t>(nn) + 1);
+    c.ne_ptr.ensure(static_cast<size_t>(nn) + 1);
+    c.ne_list.ensure(4 * static_cast<size_t>(ne) + 1);
+    LF_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int) * (nn + 1), c.stream));
+    LF_CUDA(cudaMemsetAsync(fill.p, 0, sizeof(int) * (nn + 1), c.stream));
+    if (ne > 0) count_node_elems<<<grid_e, kThreads, 0, c.stream>>>(ne, c.elem_nodes, cnt);
+    exclusive_scan(c, cnt, c.ne_ptr, nn + 1, tmp);
+    if (ne > 0) fill_node_elems<<<grid_e, kThreads, 0, c.stream>>>(ne, c.elem_nodes, c.ne_ptr, fill, c.ne_list);
+    sort_node_elems<<<grid_n, kThreads, 0, c.stream>>>(nn, c.ne_ptr, c.ne_list);
+    c.launches += 3;
+    LF_CUDA(cudaGetLastError());
+    c.ne_version = c.mesh_version;
+}
 
 bool build_pattern_device(Context& c, std::vector<int>& rowptr_host) {
     const int nn = static_cast<int>(c.n_nodes), ne = static_cast<int>(c.n_elem);

@@ -10,11 +10,12 @@ liblfgpu through the C ABI:
     retain K, f; Dirichlet; zero-pivot sweep         lfgpu_apply_dirichlet
     solve_iterative (src/solver.cpp:675-747)         lfgpu_solve
     reactions (src/solver.cpp:953-954)               lfgpu_reactions
+    postprocess + smoothing (src/solver.cpp:756-871) lfgpu_postprocess
 
 Errors keep the reference's wording and exception kinds: a failed solve raises
 ``RuntimeError`` with the message ``pcg_solve`` throws, non-convergence raises
 ``RuntimeError("PCG did not converge: ...")`` (src/solver.cpp:948-950).
-Post-processing and VTK/CSV output stay with the reference host library.
+VTK/CSV output stays with the reference host library.
 """
 
 from __future__ import annotations
@@ -84,12 +85,20 @@ class PerformanceReport:
 
 @dataclass
 class AnalysisResult:
+    """``AnalysisResult`` (include/lightfem/solver.hpp:76-86).  ``element_results``
+    is E x 5 x 7 in element order: the centre, then the Gauss points (-g,-g),
+    (g,-g), (g,g), (-g,g), each strain xx, yy, xy, stress xx, yy, xy, von Mises
+    (ElementResult); ``node_results`` is N x 4 in node order: smoothed stress xx,
+    yy, xy and von Mises (NodeResult)."""
+
     stiffness: CsrMatrix | None
     load: np.ndarray
     displacement: np.ndarray
     reaction: np.ndarray
     solver: LinearSolverReport
     performance: PerformanceReport = field(default_factory=PerformanceReport)
+    element_results: np.ndarray | None = None
+    node_results: np.ndarray | None = None
 
 
 _MESSAGES = {
@@ -121,9 +130,10 @@ def upload_model(ctx: _native.Context, model: Model) -> None:
 class LinearElasticSolver:
     """GPU drop-in for ``lightfem::LinearElasticSolver`` (include/lightfem/solver.hpp:89-92)."""
 
-    def __init__(self, device: int = 0, retain_matrix: bool = True):
+    def __init__(self, device: int = 0, retain_matrix: bool = True, postprocess: bool = True):
         self.device = device
         self.retain_matrix = retain_matrix
+        self.postprocess = postprocess
         self.context: _native.Context | None = None
 
     def solve(self, model: Model) -> AnalysisResult:
@@ -161,13 +171,19 @@ class LinearElasticSolver:
         if not report.converged:
             raise RuntimeError("PCG did not converge: " + report.message)
         reaction = ctx.reactions()
+        fields = nodal = None
+        if self.postprocess:
+            try:
+                fields, nodal = ctx.postprocess()
+            except _native.GpuError as err:
+                raise RuntimeError(str(err)) from err
         tm = ctx.timings()
         perf.assembly = strategy
         perf.coloring_count = tm["coloring_count"]
         perf.pattern_ms = tm["pattern_ms"]
         perf.assembly_ms = tm["assembly_ms"]
         perf.boundary_ms = tm["boundary_ms"]
-        perf.postprocess_ms = tm["reactions_ms"]
+        perf.postprocess_ms = tm["reactions_ms"] + (tm["postprocess_ms"] if self.postprocess else 0.0)
         stiffness = None
         if self.retain_matrix:
             rp, col, _, _ = ctx.download_pattern()
@@ -175,4 +191,4 @@ class LinearElasticSolver:
         load = ctx.download(_native.F_FULL)
         perf.total_ms = (time.perf_counter() - t0) * 1e3
         return AnalysisResult(stiffness=stiffness, load=load, displacement=u, reaction=reaction, solver=report,
-                              performance=perf)
+                              performance=perf, element_results=fields, node_results=nodal)

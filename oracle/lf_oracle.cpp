@@ -917,6 +917,88 @@ int lfo_adjoint_grad(const double* xy, i64 n_elem, const i64* nodes, const doubl
 // reverse_cuthill_mckee, src/reordering.cpp:11-62: node adjacency through Q4
 // elements, seeds and neighbours ordered by (degree, node ID), BFS, reversed.
 // ids[] are node IDs (any order); elem[] holds node IDs.  order[] receives IDs.
+// Element fields and nodal stress smoothing: q4_center_field and
+// q4_gauss_point_fields (src/element.cpp:212-248) as postprocess calls them
+// (src/solver.cpp:756-771), and smooth_nodal_stresses (src/solver.cpp:807-871).
+// fields[35 e + 7 k + (0..6)] = strain (3), stress (3), von Mises for k = 0 the
+// element centre and k = 1..4 the Gauss points (-g,-g), (g,-g), (g,g), (-g,g);
+// nodal[4 i + (0..3)] = smoothed stress (3) and its von Mises.  Returns -1 for a
+// non-positive Jacobian.
+int lfo_postprocess(const double* xy, i64 n_nodes, i64 n_elem, const i64* nodes, const double* young,
+                    const double* poisson, int plane_strain, const double* u, double* fields, double* nodal) {
+    auto field = [](const double b[24], const double d[9], const double ue[8], double* out) {
+        double strain[3] = {0.0, 0.0, 0.0}, stress[3] = {0.0, 0.0, 0.0};
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 8; ++c) strain[r] += b[8 * r + c] * ue[c];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) stress[r] += d[3 * r + c] * strain[c];
+        const double sx = stress[0], sy = stress[1], txy = stress[2];
+        out[0] = strain[0];
+        out[1] = strain[1];
+        out[2] = strain[2];
+        out[3] = sx;
+        out[4] = sy;
+        out[5] = txy;
+        out[6] = std::sqrt(std::max(0.0, sx * sx - sx * sy + sy * sy + 3.0 * txy * txy));
+    };
+    int bad = 0;
+#pragma omp parallel for schedule(static)
+    for (i64 e = 0; e < n_elem; ++e) {
+        double exy[8], ue[8], d[9], b[24], det;
+        for (int a = 0; a < 4; ++a) {
+            const i64 nd = nodes[4 * e + a];
+            exy[2 * a] = xy[2 * nd];
+            exy[2 * a + 1] = xy[2 * nd + 1];
+            ue[2 * a] = u[2 * nd];
+            ue[2 * a + 1] = u[2 * nd + 1];
+        }
+        constitutive(young[e], poisson[e], plane_strain, d);
+        double* out = fields + 35 * e;
+        if (!kinematics(exy, 0.0, 0.0, b, &det)) {
+#pragma omp atomic write
+            bad = 1;
+            continue;
+        }
+        field(b, d, ue, out);
+        for (int g = 0; g < 4; ++g) {
+            if (!kinematics(exy, kPoints[g][0], kPoints[g][1], b, &det)) {
+#pragma omp atomic write
+                bad = 1;
+                break;
+            }
+            field(b, d, ue, out + 7 * (g + 1));
+        }
+    }
+    if (bad) return -1;
+    constexpr double root_three = 1.7320508075688772935;
+    const double alpha = 0.5 * (1.0 + root_three);
+    const double beta = 0.5 * (1.0 - root_three);
+    const double ext[4][4] = {{alpha * alpha, alpha * beta, beta * beta, alpha * beta},
+                              {alpha * beta, alpha * alpha, alpha * beta, beta * beta},
+                              {beta * beta, alpha * beta, alpha * alpha, alpha * beta},
+                              {alpha * beta, beta * beta, alpha * beta, alpha * alpha}};
+    std::vector<double> sums(3 * static_cast<size_t>(n_nodes), 0.0);
+    std::vector<i64> counts(static_cast<size_t>(n_nodes), 0);
+    for (i64 e = 0; e < n_elem; ++e)
+        for (int a = 0; a < 4; ++a) {
+            const i64 nd = nodes[4 * e + a];
+            for (int c = 0; c < 3; ++c)
+                for (int g = 0; g < 4; ++g) sums[3 * nd + c] += ext[a][g] * fields[35 * e + 7 * (g + 1) + 3 + c];
+            ++counts[nd];
+        }
+    for (i64 i = 0; i < n_nodes; ++i) {
+        double* out = nodal + 4 * i;
+        if (counts[i] == 0) {
+            out[0] = out[1] = out[2] = out[3] = 0.0;
+            continue;
+        }
+        for (int c = 0; c < 3; ++c) out[c] = sums[3 * i + c] / static_cast<double>(counts[i]);
+        const double sx = out[0], sy = out[1], txy = out[2];
+        out[3] = std::sqrt(std::max(0.0, sx * sx - sx * sy + sy * sy + 3.0 * txy * txy));
+    }
+    return 0;
+}
+
 void lfo_rcm(i64 n_nodes, const i64* ids, i64 n_elem, const i64* elem, i64* order) {
     std::vector<i64> sorted(ids, ids + n_nodes);
     std::sort(sorted.begin(), sorted.end());

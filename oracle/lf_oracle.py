@@ -51,6 +51,7 @@ def lib() -> ctypes.CDLL:
             "lfo_precond_apply": (i32, [i64, vp, vp, vp, i32, i32, i64, vp, vp, vp, vp]),
             "lfo_pcg": (i32, [i64, vp, vp, vp, vp, d, i64, i32, i32, i32, i64, vp, vp, vp, vp, i64]),
             "lfo_adjoint_grad": (i32, [vp, i64, vp, vp, vp, vp, i32, vp, vp, vp]),
+            "lfo_postprocess": (i32, [vp, i64, i64, vp, vp, vp, i32, vp, vp, vp]),
             "lfo_rcm": (None, [i64, vp, i64, vp, vp]),
         }
         for name, (res, args) in sig.items():
@@ -173,6 +174,19 @@ def adjoint_grad(xy, elem_nodes, young_e, nu_e, t_e, plane_strain, u, lam) -> np
     if rc != 0:
         raise RuntimeError("non-positive Jacobian")
     return g
+
+
+def postprocess(xy, elem_nodes, young_e, nu_e, plane_strain, u):
+    """Element fields (E x 5 x 7: centre + 4 Gauss points, each strain[3], stress[3],
+    von Mises) and smoothed nodal stress (N x 4) for displacements u."""
+    xy, en = _c(xy), _c(elem_nodes, np.int64)
+    fields = np.empty((en.shape[0], 5, 7))
+    nodal = np.empty((xy.shape[0], 4))
+    rc = lib().lfo_postprocess(_p(xy), xy.shape[0], en.shape[0], _p(en), _p(_c(young_e)), _p(_c(nu_e)),
+                               int(plane_strain), _p(_c(u)), _p(fields), _p(nodal))
+    if rc != 0:
+        raise RuntimeError("Q4 stiffness evaluation received a non-positive Jacobian")
+    return fields, nodal
 
 
 def solve_model(model, *, storage=None, preconditioner=None, assembly=None, split=None, nodes_per=None,

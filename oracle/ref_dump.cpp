@@ -11,7 +11,8 @@
 //   setting overrides: assembly storage preconditioner subdomain_split
 //                      subdomain_nodes tolerance max_iterations reordering threads
 //   stages:  pattern=1 (pattern, map, colours, K, f, Kc, fc, BSR)
-//            solve=1   (u, R and the solver report through the public solve())
+//            solve=1   (u, R, element fields, smoothed nodal stress and the solver
+//                       report through the public solve())
 //            precond=1 (M^-1 fc for jacobi / 2x2 block / ic0, and the ic0 report)
 //            fd=<i,j,..> fd_step=<rel> tip_node=<id>  (central differences of the
 //                      compliance f.u and of the tip uy w.r.t. element moduli)
@@ -243,6 +244,29 @@ void stage_solve(Model model, const std::string& dir, Json& json) {
     }
     dump_f64(dir, "u", u);
     dump_f64(dir, "R", r);
+    // Element fields (element-ID order): centre then the four Gauss points, each
+    // strain[3], stress[3], von Mises; smoothed nodal stress[3] + von Mises in
+    // node-ID order.
+    std::vector<double> fields, nodal;
+    for (const ElementResult& er : result.element_results) {
+        auto put = [&](const ElementField& f) {
+            fields.insert(fields.end(), f.strain.begin(), f.strain.end());
+            fields.insert(fields.end(), f.stress.begin(), f.stress.end());
+            fields.push_back(f.von_mises);
+        };
+        put(er.field);
+        for (const auto& gp : er.gauss_points) put(gp.field);
+    }
+    std::vector<std::pair<int, const NodeResult*>> nodes_by_id;
+    for (const NodeResult& nr : result.node_results) nodes_by_id.emplace_back(nr.node_id, &nr);
+    std::sort(nodes_by_id.begin(), nodes_by_id.end());
+    for (const auto& [id, nr] : nodes_by_id) {
+        (void)id;
+        nodal.insert(nodal.end(), nr->stress.begin(), nr->stress.end());
+        nodal.push_back(nr->von_mises);
+    }
+    dump_f64(dir, "post_fields", fields);
+    dump_f64(dir, "post_nodal", nodal);
     json.num("iterations", static_cast<double>(result.solver.iterations));
     json.num("initial_residual", result.solver.initial_residual);
     json.num("final_residual", result.solver.final_residual);

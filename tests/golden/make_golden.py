@@ -19,8 +19,13 @@ Cases:
   strain     16x8 plane-strain cantilever with RCM (the 1000x1000 workload's physics)
   adjoint    20x20 cantilever with log-normal per-element moduli + reference FD
   cfg1       the 200x200 workload: iteration counts, residuals, sampled u and R
-  cfg2       the 1000x1000 workload: known answers from the reference (optional,
-             read from _work/big/cfg2_<variant> when those long runs exist)
+  cfg2       the 1000x1000 workload: known answers from the reference.  These runs
+             take hours; `--run-cfg2 DIR` makes them (ref_dump output per variant
+             in DIR/cfg2_<variant>) and `--cfg2-dir DIR` reads them back.  Without
+             either, the cfg2 entries already in golden.json and cfg2.npz are kept.
+
+Solve runs also carry the reference's post-processing (element centre and Gauss
+point fields, smoothed nodal stress); the small cases keep them.
 """
 
 from __future__ import annotations
@@ -96,11 +101,26 @@ VARIANTS = {
 }
 
 
+# The 1000x1000 runs: the reference's settings for each stored variant.
+CFG2_VARIANTS = {
+    "jacobi": ("storage=csr", "preconditioner=jacobi", "assembly=coloring"),
+    "bsr_jacobi": ("storage=bsr", "preconditioner=jacobi", "assembly=coloring"),
+    "block": ("storage=bsr", "preconditioner=block", "subdomain_split=chunk", "subdomain_nodes=1",
+              "assembly=coloring"),
+    "ic0": ("storage=csr", "preconditioner=ic0", "assembly=coloring"),
+}
+
+
 def save(name: str, arrays: dict) -> None:
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **arrays)
 
 
 def main() -> None:
+    import argparse
+    ap = argparse.ArgumentParser(description="regenerate tests/golden from the reference's sources")
+    ap.add_argument("--cfg2-dir", help="read the 1000x1000 reference runs from this directory")
+    ap.add_argument("--run-cfg2", help="make the 1000x1000 reference runs in this directory (hours)")
+    args = ap.parse_args()
     if not os.path.exists(REF_DUMP):
         raise SystemExit("build the reference first: make -C oracle ref")
     golden: dict = {}
@@ -112,6 +132,8 @@ def main() -> None:
         col_arrays, col_report = run(model, "pattern=1", "assembly=coloring", "solve=1")
         arrays["K_coloring"] = col_arrays["K"]
         arrays["u_coloring"] = col_arrays["u"]
+        for k in ("post_fields", "post_nodal"):
+            arrays[k] = arrays[k].reshape(-1, 5, 7) if k == "post_fields" else arrays[k].reshape(-1, 4)
         report["coloring"] = col_report
         if name == "scrambled":
             rcm_arrays, rcm_report = run(model, "pattern=1", "reordering=rcm", "solve=1")
@@ -133,6 +155,9 @@ def main() -> None:
         va, vr = run(model, "solve=1", *opts)
         arrays[f"u_{vname}"] = va["u"]
         arrays[f"R_{vname}"] = va["R"]
+        if vname == "csr_jacobi":
+            arrays["post_fields"] = va["post_fields"].reshape(-1, 5, 7)
+            arrays["post_nodal"] = va["post_nodal"].reshape(-1, 4)
         golden["grid6"][vname] = vr
     save("grid6", arrays)
 
@@ -145,6 +170,9 @@ def main() -> None:
         va, vr = run(model, "solve=1", *VARIANTS[vname])
         arrays[f"u_{vname}"] = va["u"]
         arrays[f"R_{vname}"] = va["R"]
+        if vname == "csr_jacobi":
+            arrays["post_fields"] = va["post_fields"].reshape(-1, 5, 7)
+            arrays["post_nodal"] = va["post_nodal"].reshape(-1, 4)
         golden["beam"][vname] = vr
     save("beam", arrays)
 
@@ -158,6 +186,9 @@ def main() -> None:
         va, vr = run(model, "solve=1", *VARIANTS[vname])
         arrays[f"u_{vname}"] = va["u"]
         arrays[f"R_{vname}"] = va["R"]
+        if vname == "csr_jacobi":
+            arrays["post_fields"] = va["post_fields"].reshape(-1, 5, 7)
+            arrays["post_nodal"] = va["post_nodal"].reshape(-1, 4)
         golden["strain"][vname] = vr
     save("strain", arrays)
 
@@ -191,10 +222,18 @@ def main() -> None:
     save("cfg1", keep)
 
     # --- the 1000x1000 workload (long runs, made separately)
-    big = os.path.join(ROOT, "_work", "big")
     cfg2 = {}
     keep = {}
-    for vname in ("jacobi", "block", "ic0"):
+    big = args.cfg2_dir or args.run_cfg2
+    if args.run_cfg2:
+        model = mesh.workload(2)
+        with open(os.path.join(big, "cfg2.fem"), "w") as fh:
+            fh.write(mesh.to_fem(model, os.path.join(big, "out.vtk")))
+        for vname, opts in CFG2_VARIANTS.items():
+            d = os.path.join(big, f"cfg2_{vname}")
+            os.makedirs(d, exist_ok=True)
+            subprocess.run([REF_DUMP, os.path.join(big, "cfg2.fem"), d, "solve=1", *opts], check=True)
+    for vname in (CFG2_VARIANTS if big else ()):
         d = os.path.join(big, f"cfg2_{vname}")
         if os.path.exists(os.path.join(d, "report.json")):
             with open(os.path.join(d, "report.json")) as fh:

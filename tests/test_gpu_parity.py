@@ -205,6 +205,25 @@ def test_preconditioner_applications(native, oracle, name):
         assert ms > 0.0
 
 
+@pytest.mark.parametrize("name", ["grid6", "beam", "strain"])
+def test_postprocess_fields(native, oracle, name):
+    """Element fields and smoothed nodal stress on the device: bit for bit the
+    oracle's for the same displacements, and the reference's (from its own
+    displacements) within the solve tolerance."""
+    g = load_golden(name)
+    model = indexed(CASES[name]())
+    res = LinearElasticSolver().solve(model)
+    en = model.element_node_index()
+    mi = model.material_index(model.element_material)
+    fields, nodal = oracle.postprocess(model.xy, en, model.young[mi], model.poisson[mi], model.settings.plane_mode,
+                                       res.displacement)
+    np.testing.assert_array_equal(res.element_results, fields)
+    np.testing.assert_array_equal(res.node_results, nodal)
+    by_id = np.argsort(model.node_ids, kind="stable")
+    assert rel(res.element_results, g["post_fields"]) <= 1e-7
+    assert rel(res.node_results[by_id], g["post_nodal"]) <= 1e-7
+
+
 def test_ic0_rejects_mixed_precision(native):
     model = indexed(CASES["grid6"]())
     model.settings.preconditioner, model.settings.precision = "ic0", "mixed"

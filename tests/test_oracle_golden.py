@@ -178,3 +178,18 @@ def test_adjoint_gradient_against_reference_fd(oracle, golden_json):
     # the GPU gradient is held to 1e-6 against this restatement instead.
     np.testing.assert_allclose(grad_c[el], g["fd_dc_dE"], rtol=1e-4)
     np.testing.assert_allclose(grad_t[el], g["fd_dtip_dE"], rtol=1e-4, atol=1e-4 * np.abs(g["fd_dtip_dE"]).max())
+
+
+@pytest.mark.parametrize("name", ["single_q4", "scrambled", "grid6", "beam", "strain"])
+def test_postprocess_matches_reference(oracle, name):
+    """Element centre / Gauss-point fields and smoothed nodal stress from the
+    reference's own displacements: bit for bit (src/element.cpp:212-248,
+    src/solver.cpp:756-871)."""
+    g = load_golden(name)
+    model = indexed(CASES[name]())  # node-ID order, as the golden vectors are stored
+    u = g["u"] if "u" in g else g["u_csr_jacobi"]
+    en = model.element_node_index()
+    mi = model.material_index(model.element_material)
+    fields, nodal = oracle.postprocess(model.xy, en, model.young[mi], model.poisson[mi], model.settings.plane_mode, u)
+    np.testing.assert_array_equal(fields, g["post_fields"])
+    np.testing.assert_array_equal(nodal, g["post_nodal"])
