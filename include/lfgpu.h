@@ -141,6 +141,7 @@ typedef struct lfgpu_timings {
     int64_t coloring_count;  /* colours used by the colouring strategy */
     int64_t kernel_launches; /* kernels this handle has launched so far (graph nodes included) */
     double postprocess_ms;   /* element fields + nodal smoothing (lfgpu_postprocess) */
+    double rcm_ms;           /* lfgpu_rcm (host wall time, device work included) */
 } lfgpu_timings;
 
 /* --- handle ------------------------------------------------------------------- */
@@ -256,6 +257,12 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* opt
 int lfgpu_residual_norm_noalloc(int64_t n_rows, const int32_t* row_offsets, const int32_t* columns,
                                 const double* values, const double* u, const double* f, void* stream,
                                 double* norm_out);
+
+/* Reverse Cuthill-McKee order of the handle's mesh (reverse_cuthill_mckee,
+ * src/reordering.cpp:11-62), computed on the device: order_out[n_nodes] receives
+ * node indices of the mesh given to lfgpu_set_mesh.  The reference ranks ties by
+ * node ID, so pass the nodes in ascending-ID order to get the reference's order. */
+int lfgpu_rcm(lfgpu_t h, int64_t* order_out);
 
 /* --- host utilities (setup the reference performs on the host) ----------------- */
 /* reverse_cuthill_mckee (src/reordering.cpp:11-62): node IDs in the new order. */

@@ -55,7 +55,7 @@ class Report(ctypes.Structure):
 class Timings(ctypes.Structure):
     _fields_ = [("pattern_ms", c_double), ("assembly_ms", c_double), ("boundary_ms", c_double),
                 ("reactions_ms", c_double), ("coloring_count", c_int64), ("kernel_launches", c_int64),
-                ("postprocess_ms", c_double)]
+                ("postprocess_ms", c_double), ("rcm_ms", c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -97,6 +97,7 @@ _SIGNATURES = {
     "lfgpu_spmv": (c_int, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, POINTER(c_double)]),
     "lfgpu_adjoint": (c_int, [c_void_p, c_void_p, POINTER(SolveOptions), c_void_p, POINTER(Report)]),
     "lfgpu_postprocess": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "lfgpu_rcm": (c_int, [c_void_p, c_void_p]),
     "lfgpu_apply_preconditioner": (c_int, [c_void_p, c_int32, c_void_p, c_void_p, POINTER(c_double)]),
     "lfgpu_residual_norm_noalloc": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                             POINTER(c_double)]),
@@ -316,6 +317,12 @@ class Context:
         self._check(self._lib.lfgpu_spmv(self._h, which, STORAGE[storage], PRECISION[precision], _ptr(x), _ptr(y),
                                          int(repeat), ctypes.byref(ms)))
         return y, ms.value
+
+    def rcm(self) -> np.ndarray:
+        """Reverse Cuthill-McKee order of this mesh's node indices, on the device."""
+        out = np.empty(self.n_dofs // 2, np.int64)
+        self._check(self._lib.lfgpu_rcm(self._h, _ptr(out)))
+        return out
 
     def postprocess(self):
         """Element fields (E x 5 x 7: centre + 4 Gauss points; strain xx, yy, xy,

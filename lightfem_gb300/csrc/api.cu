@@ -8,6 +8,7 @@
 #include <cstring>
 #include <exception>
 #include <new>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -913,6 +914,24 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
         LF_CUDA(cudaMemcpyAsync(grad, gd, sizeof(double) * h->n_elem, cudaMemcpyDeviceToHost, h->stream));
         check_status(*h);
         if (rep) *rep = r;
+    });
+}
+
+int lfgpu_rcm(lfgpu_t h, int64_t* order_out) {
+    return guarded(h, [&] {
+        LF_REQUIRE(h->n_nodes > 0, LFGPU_ERR_STATE, "set the mesh before ordering it");
+        LF_REQUIRE(order_out != nullptr, LFGPU_ERR_ARGUMENT, "null order output");
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<int> order;
+        if (rcm_device(*h, order)) {
+            for (i64 k = 0; k < h->n_nodes; ++k) order_out[k] = order[static_cast<size_t>(k)];
+        } else {  // a level or a node valence beyond the device search: order on the host
+            std::vector<long long> ids(static_cast<size_t>(h->n_nodes));
+            std::iota(ids.begin(), ids.end(), 0LL);
+            std::vector<long long> en(h->h_elem_nodes.begin(), h->h_elem_nodes.end());
+            rcm_order(h->n_nodes, ids.data(), h->n_elem, en.data(), reinterpret_cast<long long*>(order_out));
+        }
+        h->timings.rcm_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     });
 }
 

@@ -65,6 +65,9 @@ void ensure_ic0(Context& c);
 bool build_pattern_device(Context& c, std::vector<int>& rowptr_host);
 // node -> elements lists in ascending element order, cached per mesh (c.ne_ptr, c.ne_list)
 void ensure_node_elements(Context& c);
+// Reverse Cuthill-McKee order of the mesh's node indices; false if a level is wider
+// than the device search takes (the caller orders on the host)
+bool rcm_device(Context& c, std::vector<int>& order);
 
 // postprocess.cu: element fields (35 per element) and smoothed nodal stress (4 per node)
 void launch_postprocess(Context& c, const double* u, double* fields, double* nodal);

@@ -18,6 +18,7 @@
 #include "common.cuh"
 #include "kernels.hpp"
 
+#include <algorithm>
 #include <vector>
 
 namespace lfgpu {
@@ -214,6 +215,154 @@ __global__ void sort_node_elems(int nn, const int* __restrict__ nptr, int* list)
     }
 }
 
+// ------------------------------------------------------------------ RCM
+// Reverse Cuthill-McKee (reverse_cuthill_mckee, src/reordering.cpp:11-62) on the
+// device, equal to the reference's order.  The adjacency of node i is S(i) minus i
+// (nodes sharing an element), each list sorted by (degree, index); seeds are taken
+// in (degree, index) order.  The breadth-first search runs level by level in one
+// CTA: every frontier node u (rank r in its level) offers each unvisited neighbour
+// v at adjacency position p the key (r, p), v keeps the smallest key, and sorting
+// the level by key reproduces the sequential queue order exactly (v is appended by
+// the first frontier node that sees it, at its position in that node's list).
+constexpr int kRcmThreads = 1024;
+constexpr int kRcmMaxLevel = 4096;  // widest level the in-CTA sort takes
+
+__global__ void rcm_degrees(int nn, const int* __restrict__ nptr, const int* __restrict__ list,
+                            const int4* __restrict__ en, int* deg, int* flags) {
+    int s[kMaxCand];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
+        const int m = node_set(i, nptr, list, en, s);
+        if (m < 0) atomicOr(flags, 1);  // too many elements at a node: the caller orders on the host
+        deg[i] = m > 0 ? m - 1 : 0;
+    }
+}
+
+__global__ void rcm_adjacency(int nn, const int* __restrict__ nptr, const int* __restrict__ list,
+                              const int4* __restrict__ en, const int* __restrict__ deg,
+                              const int* __restrict__ adj_ptr, int* adj) {
+    int s[kMaxCand];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
+        const int m = node_set(i, nptr, list, en, s);
+        int* out = adj + adj_ptr[i];
+        int k = 0;
+        for (int t = 0; t < m; ++t) {  // insertion by (degree, index)
+            const int v = s[t];
+            if (v == i) continue;
+            const int dv = deg[v];
+            int p = k;
+            while (p > 0 && (deg[out[p - 1]] > dv || (deg[out[p - 1]] == dv && out[p - 1] > v))) {
+                out[p] = out[p - 1];
+                --p;
+            }
+            out[p] = v;
+            ++k;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kRcmThreads) rcm_bfs(int nn, const int* __restrict__ adj_ptr,
+                                                       const int* __restrict__ adj, const int* __restrict__ deg,
+                                                       unsigned long long* key, unsigned char* seen, int* front_a,
+                                                       int* front_b, int* out, int* overflow) {
+    extern __shared__ unsigned long long s_key[];  // kRcmMaxLevel keys, then kRcmMaxLevel node indices
+    int* s_val = reinterpret_cast<int*>(s_key + kRcmMaxLevel);
+    __shared__ unsigned long long s_best;
+    __shared__ int s_count;
+    const int tid = threadIdx.x;
+    constexpr unsigned long long kNone = ~0ull;
+    int total = 0;  // nodes placed so far (the same in every thread)
+    int* front = front_a;
+    int* next = front_b;
+    while (true) {
+        // next seed: the unvisited node of smallest (degree, index)
+        if (tid == 0) s_best = kNone;
+        __syncthreads();
+        unsigned long long best = kNone;
+        for (int i = tid; i < nn; i += kRcmThreads)
+            if (!seen[i]) best = min(best, (static_cast<unsigned long long>(deg[i]) << 32) | static_cast<unsigned>(i));
+        for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
+        if ((tid & 31) == 0) atomicMin(&s_best, best);
+        __syncthreads();
+        if (s_best == kNone) return;
+        const int seed = static_cast<int>(s_best & 0xffffffffull);
+        if (tid == 0) {
+            seen[seed] = 1;
+            front[0] = seed;
+            out[total] = seed;
+        }
+        int width = 1;
+        total += 1;
+        __syncthreads();
+        while (true) {
+            if (tid == 0) s_count = 0;
+            __syncthreads();
+            for (int r = tid; r < width; r += kRcmThreads) {
+                const int u = front[r];
+                const int b = adj_ptr[u], e = adj_ptr[u + 1];
+                for (int p = b; p < e; ++p) {
+                    const int v = adj[p];
+                    if (seen[v]) continue;
+                    const unsigned long long k = (static_cast<unsigned long long>(r) << 32) | static_cast<unsigned>(p - b);
+                    if (atomicMin(key + v, k) == kNone) {
+                        const int slot = atomicAdd(&s_count, 1);
+                        if (slot < kRcmMaxLevel) s_val[slot] = v;
+                    }
+                }
+            }
+            __syncthreads();
+            const int m = s_count;
+            if (m == 0) break;  // this component is done
+            if (m > kRcmMaxLevel) {
+                if (tid == 0) *overflow = 1;
+                return;
+            }
+            int pw = 1;
+            while (pw < m) pw <<= 1;
+            for (int i = tid; i < pw; i += kRcmThreads) {
+                if (i < m) {
+                    s_key[i] = key[s_val[i]];
+                } else {
+                    s_key[i] = kNone;
+                    s_val[i] = -1;
+                }
+            }
+            __syncthreads();
+            for (int k2 = 2; k2 <= pw; k2 <<= 1) {  // bitonic sort by key, ascending
+                for (int j = k2 >> 1; j > 0; j >>= 1) {
+                    for (int i = tid; i < pw; i += kRcmThreads) {
+                        const int ixj = i ^ j;
+                        if (ixj > i) {
+                            const bool up = (i & k2) == 0;
+                            if ((s_key[i] > s_key[ixj]) == up) {
+                                const unsigned long long tk = s_key[i];
+                                s_key[i] = s_key[ixj];
+                                s_key[ixj] = tk;
+                                const int tv = s_val[i];
+                                s_val[i] = s_val[ixj];
+                                s_val[ixj] = tv;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            for (int i = tid; i < m; i += kRcmThreads) {
+                const int v = s_val[i];
+                next[i] = v;
+                out[total + i] = v;
+                seen[v] = 1;
+                key[v] = kNone;
+            }
+            __syncthreads();
+            total += m;
+            width = m;
+            int* t = front;
+            front = next;
+            next = t;
+        }
+    }
+}
+
 // Exclusive scan of n ints on the stream; returns the total (synchronises).
 long long exclusive_scan(Context& c, const int* in, int* out, int n, Buf<long long>& tmp) {
     const int nb = (n + kScanBlock - 1) / kScanBlock;
@@ -250,6 +399,49 @@ void ensure_node_elements(Context& c) {
     c.launches += 3;
     LF_CUDA(cudaGetLastError());
     c.ne_version = c.mesh_version;
+}
+
+bool rcm_device(Context& c, std::vector<int>& order) {
+    const int nn = static_cast<int>(c.n_nodes);
+    ensure_node_elements(c);
+    const int grid_n = grid_for(nn, kThreads, 16 * c.num_sms);
+    Buf<int> deg, adj_ptr, adj, fa, fb, out, flags;
+    Buf<unsigned long long> key;
+    Buf<unsigned char> seen;
+    Buf<long long> tmp;
+    deg.ensure(static_cast<size_t>(nn) + 1);
+    adj_ptr.ensure(static_cast<size_t>(nn) + 1);
+    flags.ensure(1);
+    LF_CUDA(cudaMemsetAsync(deg.p + nn, 0, sizeof(int), c.stream));
+    LF_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), c.stream));
+    rcm_degrees<<<grid_n, kThreads, 0, c.stream>>>(nn, c.ne_ptr, c.ne_list, c.elem_nodes, deg, flags);
+    const long long total = exclusive_scan(c, deg, adj_ptr, nn + 1, tmp);  // synchronises
+    int too_many = 0;
+    LF_CUDA(cudaMemcpy(&too_many, flags.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (too_many) return false;
+    adj.ensure(static_cast<size_t>(total) + 1);
+    rcm_adjacency<<<grid_n, kThreads, 0, c.stream>>>(nn, c.ne_ptr, c.ne_list, c.elem_nodes, deg, adj_ptr, adj);
+    key.ensure(static_cast<size_t>(nn));
+    seen.ensure(static_cast<size_t>(nn));
+    fa.ensure(kRcmMaxLevel);
+    fb.ensure(kRcmMaxLevel);
+    out.ensure(static_cast<size_t>(nn));
+    LF_CUDA(cudaMemsetAsync(key.p, 0xFF, sizeof(unsigned long long) * nn, c.stream));
+    LF_CUDA(cudaMemsetAsync(seen.p, 0, nn, c.stream));
+    LF_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int), c.stream));
+    const int smem = kRcmMaxLevel * (8 + 4);
+    LF_CUDA(cudaFuncSetAttribute(rcm_bfs, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    rcm_bfs<<<1, kRcmThreads, smem, c.stream>>>(nn, adj_ptr, adj, deg, key, seen, fa, fb, out, flags);
+    c.launches += 3;
+    LF_CUDA(cudaGetLastError());
+    int overflow = 0;
+    LF_CUDA(cudaMemcpyAsync(&overflow, flags.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    order.resize(static_cast<size_t>(nn));
+    LF_CUDA(cudaMemcpyAsync(order.data(), out.p, sizeof(int) * nn, cudaMemcpyDeviceToHost, c.stream));
+    LF_CUDA(cudaStreamSynchronize(c.stream));
+    if (overflow) return false;
+    std::reverse(order.begin(), order.end());
+    return true;
 }
 
 bool build_pattern_device(Context& c, std::vector<int>& rowptr_host) {

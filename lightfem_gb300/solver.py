@@ -4,8 +4,8 @@ Mirrors the reference's top-level solve (``LinearElasticSolver::solve``,
 src/solver.cpp:875-960) stage by stage, with every numeric stage running in
 liblfgpu through the C ABI:
 
-    reordering (RCM, src/solver.cpp:886-892)        host, lfgpu_host_rcm
-    pattern + map + colours (src/solver.cpp:228-235) host C++ inside liblfgpu
+    reordering (RCM, src/solver.cpp:886-892)        lfgpu_rcm (device)
+    pattern + map + colours (src/solver.cpp:228-235) lfgpu_build_pattern (device; colours on a host thread)
     element stiffness + assembly + loads             lfgpu_assemble
     retain K, f; Dirichlet; zero-pivot sweep         lfgpu_apply_dirichlet
     solve_iterative (src/solver.cpp:675-747)         lfgpu_solve
@@ -72,6 +72,7 @@ class LinearSolverReport:
 @dataclass
 class PerformanceReport:
     reordering: str = "none"
+    rcm_ms: float = 0.0
     assembly: str = "coloring"
     coloring_count: int = 0
     pattern_ms: float = 0.0
@@ -113,11 +114,23 @@ def solve_options(settings) -> _native.SolveOptions:
                                    settings.preconditioner, settings.precision, settings.refinement)
 
 
+def set_mesh(ctx: _native.Context, model: Model) -> None:
+    """Nodes, elements and materials of an indexed model into ``ctx``."""
+    ctx.set_mesh(model.xy, model.element_node_index(), model.material_index(model.element_material), model.young,
+                 model.poisson, model.thickness, model.settings.plane_mode)
+
+
+def rcm_order(ctx: _native.Context, model: Model) -> np.ndarray:
+    """reverse_cuthill_mckee (src/reordering.cpp:11-62) on the device: node IDs in
+    the new order.  The model must be in ascending-ID node order (sort_and_index),
+    which is how the reference ranks ties."""
+    set_mesh(ctx, model)
+    return model.node_ids[ctx.rcm()]
+
+
 def upload_model(ctx: _native.Context, model: Model) -> None:
     """Mesh, pattern, loads and constraints of an indexed model into ``ctx``."""
-    en = model.element_node_index()
-    ctx.set_mesh(model.xy, en, model.material_index(model.element_material), model.young, model.poisson,
-                 model.thickness, model.settings.plane_mode)
+    set_mesh(ctx, model)
     ctx.build_pattern()
     body_e = model.element_index(model.body_element) if model.body_element.size else None
     edge_e = model.element_index(model.edge_element) if model.edge_element.size else None
@@ -142,11 +155,12 @@ class LinearElasticSolver:
         t0 = time.perf_counter()
         s = model.settings
         perf = PerformanceReport(reordering=s.reordering)
-        if s.reordering == "rcm":
-            model.index_with_node_order(_native.host_rcm(model.node_ids, model.element_nodes))
         if self.context is None:
             self.context = _native.Context(self.device)
         ctx = self.context
+        if s.reordering == "rcm":
+            model.index_with_node_order(rcm_order(ctx, model))
+            perf.rcm_ms = ctx.timings()["rcm_ms"]
         upload_model(ctx, model)
         strategy = "atomic" if s.assembly == "atomic" or s.gpu_assembly == "atomic" else "coloring"
         ctx.assemble(strategy)

@@ -45,6 +45,23 @@ def test_pattern_map_colors_bit_exact(native, name):
     np.testing.assert_array_equal(colors, g["colors"])
 
 
+def test_rcm_on_device_matches_reference(native):
+    """lfgpu_rcm against the reference's RCM orders (golden) and against the host
+    restatement on the 1000x1000 workload and on a mesh the device search hands
+    back to the host (a node in more elements than it takes)."""
+    from cases import fan
+    from lightfem_gb300.solver import rcm_order
+    ctx = native.Context(0)
+    g = load_golden("strain")
+    model = indexed(CASES["strain"]())
+    np.testing.assert_array_equal(rcm_order(ctx, model), g["node_order"])
+    g = load_golden("scrambled")
+    model = indexed(CASES["scrambled"]())
+    np.testing.assert_array_equal(rcm_order(ctx, model), g["rcm_node_order"])
+    for model in (indexed(mesh.workload(2)), indexed(fan())):
+        np.testing.assert_array_equal(rcm_order(ctx, model), native.host_rcm(model.node_ids, model.element_nodes))
+
+
 @pytest.mark.parametrize("build", ["grid", "fan"])
 def test_pattern_builds_match_oracle(native, oracle, build):
     """The device pattern build (structured grids) and the host build it falls back
