@@ -264,6 +264,12 @@ int lfgpu_residual_norm_noalloc(int64_t n_rows, const int32_t* row_offsets, cons
  * node ID, so pass the nodes in ascending-ID order to get the reference's order. */
 int lfgpu_rcm(lfgpu_t h, int64_t* order_out);
 
+/* csr_profile (src/sparse.cpp:227-242) of the CSR pattern the handle's mesh
+ * produces, without building it: profile_out[4] = {dimension, nonzeros, bandwidth,
+ * profile}.  The reference reports it before and after RCM
+ * (PerformanceReport::before / after, src/solver.cpp:886-898). */
+int lfgpu_mesh_profile(lfgpu_t h, int64_t* profile_out);
+
 /* --- host utilities (setup the reference performs on the host) ----------------- */
 /* reverse_cuthill_mckee (src/reordering.cpp:11-62): node IDs in the new order. */
 int lfgpu_host_rcm(int64_t n_nodes, const int64_t* node_ids, int64_t n_elements,

@@ -98,6 +98,7 @@ _SIGNATURES = {
     "lfgpu_adjoint": (c_int, [c_void_p, c_void_p, POINTER(SolveOptions), c_void_p, POINTER(Report)]),
     "lfgpu_postprocess": (c_int, [c_void_p, c_void_p, c_void_p]),
     "lfgpu_rcm": (c_int, [c_void_p, c_void_p]),
+    "lfgpu_mesh_profile": (c_int, [c_void_p, c_void_p]),
     "lfgpu_apply_preconditioner": (c_int, [c_void_p, c_int32, c_void_p, c_void_p, POINTER(c_double)]),
     "lfgpu_residual_norm_noalloc": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                             POINTER(c_double)]),
@@ -317,6 +318,13 @@ class Context:
         self._check(self._lib.lfgpu_spmv(self._h, which, STORAGE[storage], PRECISION[precision], _ptr(x), _ptr(y),
                                          int(repeat), ctypes.byref(ms)))
         return y, ms.value
+
+    def mesh_profile(self) -> dict:
+        """csr_profile of the pattern this mesh produces (dimension, nonzeros,
+        bandwidth, profile), computed on the device."""
+        out = np.empty(4, np.int64)
+        self._check(self._lib.lfgpu_mesh_profile(self._h, _ptr(out)))
+        return dict(zip(("dimension", "nonzeros", "bandwidth", "profile"), (int(v) for v in out)))
 
     def rcm(self) -> np.ndarray:
         """Reverse Cuthill-McKee order of this mesh's node indices, on the device."""

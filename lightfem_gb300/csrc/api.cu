@@ -917,6 +917,33 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
     });
 }
 
+int lfgpu_mesh_profile(lfgpu_t h, int64_t* profile_out) {
+    return guarded(h, [&] {
+        LF_REQUIRE(h->n_nodes > 0, LFGPU_ERR_STATE, "set the mesh first");
+        LF_REQUIRE(profile_out != nullptr, LFGPU_ERR_ARGUMENT, "null profile output");
+        long long p[3];
+        if (!mesh_profile_device(*h, p)) {  // a node in too many elements: profile the host pattern
+            const HostPattern hp = build_pattern(h->n_nodes, h->n_elem, h->h_elem_nodes.data());
+            p[0] = hp.nnz;
+            p[1] = p[2] = 0;
+            for (i64 r = 0; r < hp.n; ++r) {
+                const i64 b = hp.rowptr[r], e = hp.rowptr[r + 1];
+                i64 lo = r;
+                for (i64 k = b; k < e; ++k) {
+                    const i64 col = hp.col[k];
+                    p[1] = std::max<long long>(p[1], col > r ? col - r : r - col);
+                    if (col <= r) lo = std::min<i64>(lo, col);
+                }
+                p[2] += r - lo;
+            }
+        }
+        profile_out[0] = 2 * h->n_nodes;
+        profile_out[1] = p[0];
+        profile_out[2] = p[1];
+        profile_out[3] = p[2];
+    });
+}
+
 int lfgpu_rcm(lfgpu_t h, int64_t* order_out) {
     return guarded(h, [&] {
         LF_REQUIRE(h->n_nodes > 0, LFGPU_ERR_STATE, "set the mesh before ordering it");

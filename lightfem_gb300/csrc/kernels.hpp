@@ -68,6 +68,9 @@ void ensure_node_elements(Context& c);
 // Reverse Cuthill-McKee order of the mesh's node indices; false if a level is wider
 // than the device search takes (the caller orders on the host)
 bool rcm_device(Context& c, std::vector<int>& order);
+// csr_profile of the pattern the mesh produces: nonzeros, bandwidth, profile; false
+// if a node has more elements than the device build handles
+bool mesh_profile_device(Context& c, long long out[3]);
 
 // postprocess.cu: element fields (35 per element) and smoothed nodal stress (4 per node)
 void launch_postprocess(Context& c, const double* u, double* fields, double* nodal);

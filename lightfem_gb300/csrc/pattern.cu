@@ -363,6 +363,46 @@ __global__ void __launch_bounds__(kRcmThreads) rcm_bfs(int nn, const int* __rest
     }
 }
 
+// csr_profile (src/sparse.cpp:227-242) of the pattern this mesh produces, from the
+// node sets alone: rows 2i and 2i+1 span columns 2 min S(i) .. 2 max S(i) + 1, a
+// node in no element keeps only its diagonal.  out: [0] nonzeros, [1] bandwidth,
+// [2] profile (64-bit sums), [3] nodes with too many elements (not counted).
+__global__ void mesh_profile(int nn, const int* __restrict__ nptr, const int* __restrict__ list,
+                             const int4* __restrict__ en, unsigned long long* out) {
+    int s[kMaxCand];
+    unsigned long long nz = 0, band = 0, prof = 0, bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
+        const int m = node_set(i, nptr, list, en, s);
+        if (m < 0) {
+            ++bad;
+            continue;
+        }
+        if (m == 0) {
+            nz += 2;
+            continue;
+        }
+        const long long lo = 2LL * s[0], hi = 2LL * s[m - 1] + 1;
+        for (int h = 0; h < 2; ++h) {
+            const long long r = 2LL * i + h;
+            nz += 2ULL * m;
+            band = max(band, static_cast<unsigned long long>(max(r - lo, hi - r)));
+            prof += static_cast<unsigned long long>(r - lo);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        nz += __shfl_xor_sync(0xffffffffu, nz, o);
+        prof += __shfl_xor_sync(0xffffffffu, prof, o);
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+        band = max(band, __shfl_xor_sync(0xffffffffu, band, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out + 0, nz);
+        atomicMax(out + 1, band);
+        atomicAdd(out + 2, prof);
+        atomicAdd(out + 3, bad);
+    }
+}
+
 // Exclusive scan of n ints on the stream; returns the total (synchronises).
 long long exclusive_scan(Context& c, const int* in, int* out, int n, Buf<long long>& tmp) {
     const int nb = (n + kScanBlock - 1) / kScanBlock;
@@ -399,6 +439,26 @@ void ensure_node_elements(Context& c) {
     c.launches += 3;
     LF_CUDA(cudaGetLastError());
     c.ne_version = c.mesh_version;
+}
+
+bool mesh_profile_device(Context& c, long long out[3]) {
+    const int nn = static_cast<int>(c.n_nodes);
+    ensure_node_elements(c);
+    Buf<unsigned long long> acc;
+    acc.ensure(4);
+    LF_CUDA(cudaMemsetAsync(acc.p, 0, 4 * sizeof(unsigned long long), c.stream));
+    mesh_profile<<<grid_for(nn, kThreads, 16 * c.num_sms), kThreads, 0, c.stream>>>(nn, c.ne_ptr, c.ne_list,
+                                                                                      c.elem_nodes, acc);
+    c.launches += 1;
+    LF_CUDA(cudaGetLastError());
+    unsigned long long h[4];
+    LF_CUDA(cudaMemcpyAsync(h, acc.p, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
+    LF_CUDA(cudaStreamSynchronize(c.stream));
+    if (h[3] != 0) return false;
+    out[0] = static_cast<long long>(h[0]);
+    out[1] = static_cast<long long>(h[1]);
+    out[2] = static_cast<long long>(h[2]);
+    return true;
 }
 
 bool rcm_device(Context& c, std::vector<int>& order) {

@@ -70,8 +70,20 @@ class LinearSolverReport:
 
 
 @dataclass
+class CsrProfile:
+    """``CsrProfile`` (include/lightfem/sparse.hpp:103-108)."""
+
+    dimension: int = 0
+    nonzeros: int = 0
+    bandwidth: int = 0
+    profile: int = 0
+
+
+@dataclass
 class PerformanceReport:
     reordering: str = "none"
+    before: CsrProfile = field(default_factory=CsrProfile)
+    after: CsrProfile = field(default_factory=CsrProfile)
     rcm_ms: float = 0.0
     assembly: str = "coloring"
     coloring_count: int = 0
@@ -159,9 +171,14 @@ class LinearElasticSolver:
             self.context = _native.Context(self.device)
         ctx = self.context
         if s.reordering == "rcm":
-            model.index_with_node_order(rcm_order(ctx, model))
+            set_mesh(ctx, model)
+            perf.before = CsrProfile(**ctx.mesh_profile())
+            model.index_with_node_order(model.node_ids[ctx.rcm()])
             perf.rcm_ms = ctx.timings()["rcm_ms"]
         upload_model(ctx, model)
+        perf.after = CsrProfile(**ctx.mesh_profile())
+        if s.reordering != "rcm":  # as the reference: "before" mirrors "after" without reordering
+            perf.before = perf.after
         strategy = "atomic" if s.assembly == "atomic" or s.gpu_assembly == "atomic" else "coloring"
         ctx.assemble(strategy)
         ctx.apply_dirichlet()

@@ -62,6 +62,34 @@ def test_rcm_on_device_matches_reference(native):
         np.testing.assert_array_equal(rcm_order(ctx, model), native.host_rcm(model.node_ids, model.element_nodes))
 
 
+def test_csr_profiles_match_reference(native, golden_json):
+    """PerformanceReport::before / after (csr_profile, src/sparse.cpp:227-242) as the
+    reference reports them: with RCM (16x8 plane strain; the 1000x1000 workload)
+    and without (the perturbed beam; the 200x200 workload, whose 405 / 32,522,001 is
+    also the reference README's known answer)."""
+    from lightfem_gb300.solver import set_mesh
+    for name in ("strain", "beam"):
+        ref = golden_json[name]["csr_jacobi"]
+        res = LinearElasticSolver().solve(indexed(CASES[name]()))
+        assert (res.performance.before.bandwidth, res.performance.before.profile) == (
+            ref["bandwidth_before"], ref["profile_before"]), name
+        assert (res.performance.after.bandwidth, res.performance.after.profile) == (
+            ref["bandwidth_after"], ref["profile_after"]), name
+    ctx = native.Context(0)
+    for cfg in (1, 2):
+        ref = golden_json[f"cfg{cfg}"]["csr_jacobi" if cfg == 1 else "jacobi"]
+        model = indexed(mesh.workload(cfg))
+        set_mesh(ctx, model)
+        before = ctx.mesh_profile()
+        if model.settings.reordering == "rcm":
+            model.index_with_node_order(model.node_ids[ctx.rcm()])
+            set_mesh(ctx, model)
+        after = ctx.mesh_profile()
+        assert (before["bandwidth"], before["profile"]) == (ref["bandwidth_before"], ref["profile_before"])
+        assert (after["bandwidth"], after["profile"]) == (ref["bandwidth_after"], ref["profile_after"])
+        assert after["nonzeros"] == ref["nnz"]
+
+
 @pytest.mark.parametrize("build", ["grid", "fan"])
 def test_pattern_builds_match_oracle(native, oracle, build):
     """The device pattern build (structured grids) and the host build it falls back
