@@ -1063,16 +1063,25 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks) {
     const cudaGraphNode_t n_loop = add_conditional(g, &n_init, 1, a->loop, cudaGraphCondTypeWhile, &body);
     cudaGraphNode_t n_flush;
     add_kernel(g, &n_flush, &n_loop, 1, mx_flush<true>, blocks, a);
-    // The IF node lives in the loop body, so its handle belongs to that graph.
-    LF_CUDA(cudaGraphConditionalHandleCreate(&a->branch, body, 0, 0));
-    cudaGraphNode_t k1, k2, k3, k4, k5;
-    add_kernel(body, &k1, nullptr, 0, mx_product<STORAGE>, blocks, a);
-    add_kernel(body, &k2, &k1, 1, mx_update<PRECOND>, blocks, a);
-    cudaGraph_t branch;
-    add_conditional(body, &k2, 1, a->branch, cudaGraphCondTypeIf, &branch);
-    add_kernel(branch, &k3, nullptr, 0, mx_flush<false>, blocks, a);
-    add_kernel(branch, &k4, &k3, 1, mx_residual<STORAGE>, blocks, a);
-    add_kernel(branch, &k5, &k4, 1, mx_reprecondition<PRECOND>, blocks, a);
+    // The body holds two iterations, halving the conditional loop's per-pass cost.
+    // Each IF node has its own handle (created on the body graph, where the nodes
+    // live); the kernels of each half carry the handle of their half, and the
+    // second half returns at once when the first one ended the solve.
+    CgArgs halves[2];  // kernel parameters are copied into the nodes at creation
+    cudaGraphNode_t prev = nullptr;
+    for (int h = 0; h < 2; ++h) {
+        halves[h] = *a;
+        CgArgs* ah = &halves[h];
+        LF_CUDA(cudaGraphConditionalHandleCreate(&ah->branch, body, 0, 0));
+        cudaGraphNode_t k1, k2, k3, k4, k5;
+        add_kernel(body, &k1, prev ? &prev : nullptr, prev ? 1 : 0, mx_product<STORAGE>, blocks, ah);
+        add_kernel(body, &k2, &k1, 1, mx_update<PRECOND>, blocks, ah);
+        cudaGraph_t branch;
+        prev = add_conditional(body, &k2, 1, ah->branch, cudaGraphCondTypeIf, &branch);
+        add_kernel(branch, &k3, nullptr, 0, mx_flush<false>, blocks, ah);
+        add_kernel(branch, &k4, &k3, 1, mx_residual<STORAGE>, blocks, ah);
+        add_kernel(branch, &k5, &k4, 1, mx_reprecondition<PRECOND>, blocks, ah);
+    }
 }
 
 // Per-kernel device time of the profiling form: an event after every launch; the
@@ -1312,8 +1321,9 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     else if (s.unrolled > 0)
         c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 5 : 3) +
                       (s.mixed ? 1 : 0);
-    else  // mixed: the branch runs flush, residual and re-preconditioning; a final flush follows the loop
-        c.launches += (s.x0 ? 1 : 0) + 1 + (s.mixed ? 2 * st.it + 3 * st.refs + 1 : 3 * st.it);
+    else  // mixed: two iterations (four kernels) a pass, the branch's flush, residual and
+          // re-preconditioning per replacement, a final flush after the loop
+        c.launches += (s.x0 ? 1 : 0) + 1 + (s.mixed ? 4 * ((st.it + 1) / 2) + 3 * st.refs + 1 : 3 * st.it);
     PcgResult r{};
     r.iterations = st.it;
     r.refinements = st.refs;
