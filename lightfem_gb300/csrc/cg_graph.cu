@@ -1055,6 +1055,8 @@ void build_fp64(cudaGraph_t g, CgArgs* a, int blocks) {
     add_kernel(body, &k3, &k2, 1, cg64_direction, blocks, a);
 }
 
+constexpr int kBodyIterations = 8;
+
 template <int STORAGE, int PRECOND>
 void build_mixed(cudaGraph_t g, CgArgs* a, int blocks) {
     cudaGraphNode_t n_init;
@@ -1063,13 +1065,13 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks) {
     const cudaGraphNode_t n_loop = add_conditional(g, &n_init, 1, a->loop, cudaGraphCondTypeWhile, &body);
     cudaGraphNode_t n_flush;
     add_kernel(g, &n_flush, &n_loop, 1, mx_flush<true>, blocks, a);
-    // The body holds two iterations, halving the conditional loop's per-pass cost.
+    // The body holds kBodyIterations iterations, dividing the conditional loop's per-pass cost.
     // Each IF node has its own handle (created on the body graph, where the nodes
     // live); the kernels of each half carry the handle of their half, and the
     // second half returns at once when the first one ended the solve.
-    CgArgs halves[2];  // kernel parameters are copied into the nodes at creation
+    CgArgs halves[kBodyIterations];  // kernel parameters are copied into the nodes at creation
     cudaGraphNode_t prev = nullptr;
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < kBodyIterations; ++h) {
         halves[h] = *a;
         CgArgs* ah = &halves[h];
         LF_CUDA(cudaGraphConditionalHandleCreate(&ah->branch, body, 0, 0));
@@ -1321,9 +1323,12 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     else if (s.unrolled > 0)
         c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 5 : 3) +
                       (s.mixed ? 1 : 0);
-    else  // mixed: two iterations (four kernels) a pass, the branch's flush, residual and
+    else  // mixed: kBodyIterations iterations (two kernels each) a pass, the branch's flush, residual and
           // re-preconditioning per replacement, a final flush after the loop
-        c.launches += (s.x0 ? 1 : 0) + 1 + (s.mixed ? 4 * ((st.it + 1) / 2) + 3 * st.refs + 1 : 3 * st.it);
+        c.launches += (s.x0 ? 1 : 0) + 1 +
+                      (s.mixed ? 2 * kBodyIterations * ((st.it + kBodyIterations - 1) / kBodyIterations) +
+                                     3 * st.refs + 1
+                               : 3 * st.it);
     PcgResult r{};
     r.iterations = st.it;
     r.refinements = st.refs;
