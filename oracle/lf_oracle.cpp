@@ -496,7 +496,7 @@ struct Report {
 
 // pcg_solve<Matrix, Preconditioner>, src/solver.cpp:532-627.  status: 0 ok/maxit,
 // 1 non-positive initial rho, 2 non-positive curvature, 3 non-positive rho.
-// ``iteration_cap`` > 0 stops early without a verdict (bounded CPU-baseline samples).
+// ``iteration_cap`` > 0 stops early without a convergence decision (bounded CPU-baseline samples).
 template <typename M>
 Report pcg(const M& a, const Precond& m, const double* b, double tol, size_t maxit, double* x, size_t iteration_cap) {
     const size_t n = a.n;
