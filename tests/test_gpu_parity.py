@@ -210,6 +210,53 @@ def test_cfg1_full_size(native, golden_json):
         assert res.solver.true_residual <= 1.01e-8 * ref[variant]["initial_residual"]
 
 
+CFG2 = {"jacobi": ("csr", "jacobi"), "bsr_jacobi": ("bsr", "jacobi"), "block": ("bsr", "block")}
+
+
+@pytest.mark.parametrize("variant", list(CFG2))
+def test_cfg2_full_size(native, golden_json, variant):
+    """The 1000x1000 workload (2,004,002 DOFs, RCM) against the reference's own runs:
+    FP64 PCG iteration count within 2, displacements within 1e-8; the mixed solve
+    reaches the same true-residual target."""
+    ref = golden_json["cfg2"][variant]
+    g = load_golden("cfg2")
+    storage, precond = CFG2[variant]
+    model = indexed(mesh.workload(2))
+    model.settings.storage, model.settings.preconditioner = storage, precond
+    res = LinearElasticSolver(retain_matrix=False, postprocess=False).solve(model)
+    assert abs(res.solver.iterations - ref["iterations"]) <= 2
+    u = by_id_order(model, res.displacement)
+    assert rel(u[::2003], g[f"u_{variant}"]) <= 1e-8
+    assert np.linalg.norm(u) == pytest.approx(ref["u_norm"], rel=1e-8)
+    assert abs(res.reaction[1::2].sum() - ref["R_y_sum"]) <= 1e-6
+    mixed = indexed(mesh.workload(2))
+    mixed.settings.storage, mixed.settings.preconditioner, mixed.settings.precision = storage, precond, "mixed"
+    rm = LinearElasticSolver(retain_matrix=False, postprocess=False).solve(mixed)
+    assert rm.solver.true_residual <= 1.001e-8 * rm.solver.initial_residual
+    assert rel(by_id_order(mixed, rm.displacement), u) <= 1e-6
+
+
+def test_cfg3_full_size_mixed_vs_fp64(native):
+    """The 2000x1000 perturbed two-material beam (4,006,002 DOFs, gravity + top
+    pressure): mixed block-Jacobi PCG with FP64 refinement and FP64 PCG both reach
+    the 1e-8 target and agree; the reactions balance the applied loads."""
+    sols = {}
+    for precision in ("fp64", "mixed"):
+        model = indexed(mesh.workload(3))
+        model.settings.storage, model.settings.preconditioner = "bsr", "block"
+        model.settings.precision = precision
+        res = LinearElasticSolver(retain_matrix=False, postprocess=False).solve(model)
+        target = 1e-8 * res.solver.initial_residual
+        if precision == "mixed":  # the refinement tests the true FP64 residual
+            assert res.solver.true_residual <= 1.001 * target
+        else:  # FP64 PCG stops on its recursive residual, as the reference does; the true one drifts a little
+            assert res.solver.final_residual <= target and res.solver.true_residual <= 1.2 * target
+        assert np.allclose(res.reaction.reshape(-1, 2).sum(axis=0), -res.load.reshape(-1, 2).sum(axis=0),
+                           rtol=1e-6, atol=1e-6 * np.abs(res.load).sum())
+        sols[precision] = res.displacement
+    assert rel(sols["mixed"], sols["fp64"]) <= 1e-6
+
+
 @pytest.mark.parametrize("storage", ["csr", "bsr"])
 @pytest.mark.parametrize("precond", ["jacobi", "block"])
 @pytest.mark.parametrize("refinement", ["reliable", "restart"])
