@@ -323,6 +323,28 @@ def test_ic0_rejects_mixed_precision(native):
         LinearElasticSolver().solve(model)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("storage", ["csr", "bsr"])
+def test_persistent_kernel(native, golden_json, precision, storage):
+    """The persistent cooperative PCG kernel (options.persistent = 1): FP64 within 2
+    iterations and 1e-8 of the reference, mixed precision at the FP64 target."""
+    variant = f"{storage}_jacobi"
+    g = load_golden("beam")
+    ref = golden_json["beam"][variant]
+    model, ctx = prepared(native, "beam")
+    ctx.assemble("coloring")
+    ctx.apply_dirichlet()
+    o = ctx.options(model.settings.tolerance, model.settings.max_iterations, storage, "jacobi", precision,
+                    persistent=1)
+    u, rep = ctx.solve(o)
+    assert rep.converged
+    if precision == "fp64":
+        assert abs(rep.iterations - ref["iterations"]) <= 2
+        assert rel(by_id_order(model, u), g[f"u_{variant}"]) <= 1e-8
+    else:
+        assert rep.true_residual <= 1.001 * model.settings.tolerance * rep.initial_residual
+
+
 def test_spmv_products(native, oracle):
     model, ctx = prepared(native, "beam")
     ctx.assemble("coloring")
