@@ -596,7 +596,7 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
             r.preconditioner_apply_ms = apply_ms;
         } else {
             LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
-            ensure_preconditioners(*h);
+            ensure_preconditioners(*h, o->preconditioner);
             LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
             r.preconditioner_setup_ms = elapsed_ms(*h);
             res = o->persistent ? run_pcg(*h, s, &ms) : run_cg_graph(*h, s, &ms);
@@ -824,7 +824,7 @@ int lfgpu_apply_preconditioner(lfgpu_t h, int32_t preconditioner, const double* 
         Buf<double>& zd = h->v64[3];
         LF_CUDA(cudaMemcpyAsync(rd.p, r, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
         if (preconditioner == LFGPU_PRECOND_IC0) ensure_ic0(*h);
-        else ensure_preconditioners(*h);
+        else ensure_preconditioners(*h, preconditioner);
         LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
         launch_precond_apply(*h, preconditioner, rd, zd);
         LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
@@ -886,7 +886,7 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
                 ensure_ic0(*h);
                 res = run_pcg_ic0(*h, s, &ms, &apply_ms);
             } else {
-                ensure_preconditioners(*h);
+                ensure_preconditioners(*h, o->preconditioner);
                 res = o->persistent ? run_pcg(*h, s, &ms) : run_cg_graph(*h, s, &ms);
             }
             double total_ms = ms;

@@ -149,6 +149,7 @@ struct Context {
     Buf<float> inv_diag32, blk32;
     unsigned long long pre_version = ~0ull;
     i64 degenerate_blocks = 0;
+    i64 nonfinite_diag = -1;  // first DOF whose diagonal is not finite, -1 if none
 
     // solve vectors and scratch
     Buf<double> u, R;

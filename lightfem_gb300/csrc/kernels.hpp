@@ -18,7 +18,9 @@ void launch_spmv_bsr32(Context& c, const float* x, float* y);
 void ensure_bsr(Context& c);                 // BSR structure + FP64 values of K (constrained)
 void ensure_bsr32(Context& c);
 void ensure_csr32(Context& c);
-void ensure_preconditioners(Context& c);     // Jacobi inverse diagonal and 2x2 nodal factors
+// Jacobi inverse diagonal and 2x2 nodal factors; raises LFGPU_ERR_NONFINITE_DIAG
+// when ``precond`` is Jacobi and a diagonal entry is not finite.
+void ensure_preconditioners(Context& c, int precond);
 void launch_to_float(Context& c, const double* in, float* out, i64 count);
 double device_norm2(Context& c, const double* v, i64 count);      // synchronous helper
 void launch_axpby(Context& c, i64 count, double a, const double* x, double b, double* y);

@@ -10,6 +10,7 @@
 #include "kernels.hpp"
 
 #include <cmath>
+#include <limits>
 
 namespace lfgpu {
 namespace {
@@ -305,14 +306,16 @@ __global__ void to_float_kernel(i64 count, const double* __restrict__ in, float*
 // SubdomainBlockJacobi (src/precond.cpp:186-231): Cholesky of
 // [[K(2i,2i), .], [K(2i+1,2i), K(2i+1,2i+1)]] with reciprocal pivots stored as
 // (1/L00, L10, 1/L11); a block that is not positive definite becomes the identity.
+// A non-finite diagonal is only an error for the Jacobi preconditioner, so the
+// kernel records the first such DOF in ``nonfinite`` and the solve decides.
 __global__ void precond_setup_kernel(int nb, const int* __restrict__ rowptr, const int* __restrict__ col,
                                      const int* __restrict__ diag, const double* __restrict__ K,
                                      double* __restrict__ inv_diag, double* __restrict__ blk,
-                                     int* __restrict__ degenerate, DeviceStatus* status) {
+                                     int* __restrict__ degenerate, int* __restrict__ nonfinite) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nb) return;
     const double d0 = K[diag[2 * i]], d1 = K[diag[2 * i + 1]];
-    if (!isfinite(d0) || !isfinite(d1)) record_failure(status, LFGPU_ERR_NONFINITE_DIAG, 2 * i);
+    if (!isfinite(d0) || !isfinite(d1)) atomicMin(nonfinite, isfinite(d0) ? 2 * i + 1 : 2 * i);
     inv_diag[2 * i] = fabs(d0) > 1.0e-30 ? 1.0 / d0 : 1.0;
     inv_diag[2 * i + 1] = fabs(d1) > 1.0e-30 ? 1.0 / d1 : 1.0;
     // K(2i+1, 2i): search row 2i+1 for column 2i.
@@ -531,28 +534,38 @@ void ensure_csr32(Context& c) {
     c.k32_version = c.k_version;
 }
 
-void ensure_preconditioners(Context& c) {
-    if (c.pre_version == c.k_version) return;
+static void setup_preconditioners(Context& c) {
     const int nb = static_cast<int>(c.n / 2);
     c.inv_diag64.ensure(c.n);
     c.blk64.ensure(3 * static_cast<size_t>(nb));
     c.inv_diag32.ensure(c.n);
     c.blk32.ensure(3 * static_cast<size_t>(nb));
     c.scratch64.ensure(64);
-    int* degenerate = reinterpret_cast<int*>(c.scratch64.p + 8);
-    LF_CUDA(cudaMemsetAsync(degenerate, 0, sizeof(int), c.stream));
+    // flags[0]: degenerate 2x2 blocks; flags[1]: first non-finite diagonal DOF.
+    int* flags = reinterpret_cast<int*>(c.scratch64.p + 8);
+    static const int init[2] = {0, std::numeric_limits<int>::max()};
+    LF_CUDA(cudaMemcpyAsync(flags, init, sizeof(init), cudaMemcpyHostToDevice, c.stream));
     precond_setup_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(nb, c.rowptr, c.col, c.diag, c.K,
-                                                                           c.inv_diag64, c.blk64, degenerate,
-                                                                           c.status);
+                                                                           c.inv_diag64, c.blk64, flags,
+                                                                           flags + 1);
     c.launches += 1;
     LF_CUDA(cudaGetLastError());
     launch_to_float(c, c.inv_diag64, c.inv_diag32, c.n);
     launch_to_float(c, c.blk64, c.blk32, 3LL * nb);
-    int h = 0;
-    LF_CUDA(cudaMemcpyAsync(&h, degenerate, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    int h[2] = {0, 0};
+    LF_CUDA(cudaMemcpyAsync(h, flags, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
     check_status(c);
-    c.degenerate_blocks = h;
+    c.degenerate_blocks = h[0];
+    c.nonfinite_diag = h[1] == std::numeric_limits<int>::max() ? -1 : h[1];
     c.pre_version = c.k_version;
+}
+
+void ensure_preconditioners(Context& c, int precond) {
+    if (c.pre_version != c.k_version) setup_preconditioners(c);
+    // inverse_diagonal_of, src/solver.cpp:656-669: only the Jacobi setup checks.
+    if (precond == LFGPU_PRECOND_JACOBI && c.nonfinite_diag >= 0)
+        throw Error{LFGPU_ERR_NONFINITE_DIAG, "Jacobi preconditioner encountered a non-finite diagonal (dof " +
+                                                  std::to_string(c.nonfinite_diag) + ")"};
 }
 
 double device_norm2(Context& c, const double* v, i64 count) {

@@ -17,6 +17,14 @@
 //            fd=<i,j,..> fd_step=<rel> tip_node=<id>  (central differences of the
 //                      compliance f.u and of the tip uy w.r.t. element moduli)
 //            ke=<count> (element matrices of the first <count> elements)
+//            outcome=1 (the public solve() once: "converged" with its iterations
+//                       and u, or the message of the exception it throws)
+//   library-level inputs (the solver needs only an indexed model,
+//   src/solver.cpp:876-878; the parser and validator refuse these values):
+//            validate=0          skip ModelValidator
+//            set_young=<id>:<v>  Young's modulus of material <id> after parsing
+//            set_fy=<id>:<v>     fy of the nodal load at node <id> after parsing
+//            (<v> is read with strtod, so nan and inf are accepted)
 #include "src/solver.cpp"
 
 #include "lightfem/input_parser.hpp"
@@ -81,10 +89,34 @@ Model load(const std::string& path, const std::map<std::string, std::string>& op
         else if (key == "reordering") s.reordering = value;
         else if (key == "threads") s.threads = std::stoull(value);
     }
-    const lightfem::ValidationReport report = lightfem::ModelValidator{}.validate(model);
-    if (!report.ok()) {
-        for (const auto& d : report.diagnostics()) std::fprintf(stderr, "%s: %s\n", d.code.c_str(), d.message.c_str());
-        throw std::runtime_error("model did not pass the reference validation");
+    for (const auto& [key, value] : opt) {
+        if (key != "set_young" && key != "set_fy") continue;
+        const std::size_t colon = value.find(':');
+        const int id = std::stoi(value.substr(0, colon));
+        const double v = std::strtod(value.c_str() + colon + 1, nullptr);
+        bool found = false;
+        if (key == "set_young") {
+            for (auto& m : model.materials) {
+                if (m.id != id) continue;
+                m.young_modulus = v;
+                found = true;
+            }
+        } else {
+            for (auto& l : model.loads) {
+                if (l.node_id != id) continue;
+                l.fy = v;
+                found = true;
+            }
+        }
+        if (!found) throw std::runtime_error(key + ": no record with id " + std::to_string(id));
+    }
+    if (!opt.count("validate") || opt.at("validate") != "0") {
+        const lightfem::ValidationReport report = lightfem::ModelValidator{}.validate(model);
+        if (!report.ok()) {
+            for (const auto& d : report.diagnostics())
+                std::fprintf(stderr, "%s: %s\n", d.code.c_str(), d.message.c_str());
+            throw std::runtime_error("model did not pass the reference validation");
+        }
     }
     model.sort_and_index();
     return model;
@@ -336,6 +368,28 @@ void stage_fd(const Model& base, const std::string& dir, const std::string& list
 
 }  // namespace
 
+// One public solve(): the outcome the GPU path's failure tests compare with.
+void stage_outcome(Model model, const std::string& dir, Json& json) {
+    using namespace lightfem;
+    try {
+        const AnalysisResult result = LinearElasticSolver{}.solve(model);
+        json.str("outcome", "converged");
+        json.num("iterations", static_cast<double>(result.solver.iterations));
+        std::vector<std::pair<int, std::size_t>> by_id;
+        for (const Node& node : model.nodes) by_id.emplace_back(node.id, node.dof_x);
+        std::sort(by_id.begin(), by_id.end());
+        std::vector<double> u;
+        for (const auto& [id, dof] : by_id) {
+            (void)id;
+            u.push_back(result.displacement[dof]);
+            u.push_back(result.displacement[dof + 1]);
+        }
+        dump_f64(dir, "u", u);
+    } catch (const std::runtime_error& error) {
+        json.str("outcome", error.what());
+    }
+}
+
 int main(int argc, char** argv) {
     if (argc < 3) {
         std::fprintf(stderr, "usage: ref_dump <model.fem> <outdir> [key=value ...]\n");
@@ -355,6 +409,7 @@ int main(int argc, char** argv) {
         if (opt.count("pattern")) stage_pattern(model, dir, json, opt.count("ke") ? std::stoull(opt["ke"]) : 0);
         if (opt.count("precond")) stage_precond(model, dir, json);
         if (opt.count("solve")) stage_solve(model, dir, json);
+        if (opt.count("outcome")) stage_outcome(model, dir, json);
         if (opt.count("fd")) {
             stage_fd(model, dir, opt["fd"], opt.count("fd_step") ? std::stod(opt["fd_step"]) : 1e-6,
                      opt.count("tip_node") ? std::stoi(opt["tip_node"]) : 1, json);

@@ -73,6 +73,122 @@ def fan(sectors: int = 20) -> Model:
                  settings=SolverSettings(tolerance=1e-12, max_iterations=1000))
 
 
+def element_moduli(model, element, value):
+    """grid6 with one material per element and ``value`` as element ``element``'s modulus."""
+    ne = model.element_ids.shape[0]
+    young = np.full(ne, 1.0e6)
+    young[element] = value
+    model.material_ids = np.arange(1, ne + 1)
+    model.young, model.poisson, model.thickness = young, np.full(ne, 0.25), np.ones(ne)
+    model.element_material = np.arange(1, ne + 1)
+    return model
+
+
+def huge_thickness(model, element, value):
+    """grid6 with element ``element`` ``value`` thick: its K_e overflows to +inf on
+    the diagonal whichever order the products are taken in."""
+    model = element_moduli(model, element, 1.0e6)
+    model.thickness[element] = value
+    return model
+
+
+def floating_node(model, loaded):
+    """grid6 plus a node that belongs to no element (zero rows of K)."""
+    new_id = int(model.node_ids.max()) + 1
+    model.node_ids = np.append(model.node_ids, new_id)
+    model.xy = np.vstack([model.xy, [9.0, 9.0]])
+    if loaded:
+        model.load_node = np.append(model.load_node, new_id)
+        model.load_fx = np.append(model.load_fx, 0.0)
+        model.load_fy = np.append(model.load_fy, -1.0)
+    return model
+
+
+def with_load(value):
+    def make():
+        m = grid6()
+        m.load_fy[0] = value
+        return m
+    return make
+
+
+def _zero_loads(m):
+    m.load_fy[:] = 0.0
+    return m
+
+
+# Models on which the reference's solve stops, or finishes, in one known way (the
+# zero-pivot sweep, the Jacobi setup, pcg_solve's three checks, or the "initial
+# residual satisfies tolerance" exit).
+FAILURE_MODELS = {
+    "nan_load": with_load(np.nan),               # r0 = sqrt(max(0, NaN)) = 0: converged at once
+    "inf_load": with_load(np.inf),               # r0 = inf <= tol * inf: converged at once
+    "zero_load": lambda: _zero_loads(grid6()),
+    "nan_modulus": lambda: element_moduli(grid6(), 14, np.nan),      # NaN pivots swept to 1
+    "nan_modulus_loaded": lambda: element_moduli(grid6(), 35, np.nan),  # ... one of them loaded
+    "huge_thickness": lambda: huge_thickness(grid6(), 14, 1.0e307),  # +inf diagonal survives
+    "negative_modulus_half": lambda: element_moduli(grid6(), 14, -0.5e6),
+    "negative_modulus_1": lambda: element_moduli(grid6(), 14, -1.0e6),
+    "negative_modulus_5": lambda: element_moduli(grid6(), 14, -5.0e6),
+    "negative_modulus_50": lambda: element_moduli(grid6(), 14, -5.0e7),
+    "floating_node": lambda: floating_node(grid6(), loaded=False),
+    "floating_node_loaded": lambda: floating_node(grid6(), loaded=True),
+}
+
+# Failure cases whose outcome is fixed before the first search direction is formed
+# or at its first product, so an FP32 inner loop must end the same way.
+FAILURE_DETERMINISTIC = {"nan_load", "inf_load", "zero_load", "nan_modulus", "nan_modulus_loaded",
+                         "huge_thickness", "floating_node", "floating_node_loaded"}
+_ORACLE_STATUS = {1: "rho_initial", 2: "not_spd", 3: "rho"}
+
+
+def failure_case(name, storage, precond):
+    """A failure model, indexed, with the storage and preconditioner set (block =
+    2x2 nodal blocks)."""
+    m = FAILURE_MODELS[name]()
+    m.settings.storage, m.settings.preconditioner = storage, precond
+    m.settings.subdomain_split, m.settings.subdomain_nodes = "chunk", 1
+    return indexed(m)
+
+
+# The reference's exception messages (src/solver.cpp:579-581, :591-593, :616-618,
+# :656-669, :926-936) by the kind the failure tests compare.
+_OUTCOME_TEXT = {
+    "mechanism": "the structure is a mechanism",
+    "nonfinite_diag": "Jacobi preconditioner encountered a non-finite diagonal",
+    "rho_initial": "PCG failed to form a positive initial preconditioned residual",
+    "not_spd": "PCG encountered non-positive curvature; system is not SPD",
+    "rho": "PCG preconditioned residual became non-positive or non-finite",
+}
+
+
+def outcome_kind(message: str) -> str:
+    """The kind of a reference solve() outcome ("converged" or an exception message)."""
+    if message == "converged":
+        return message
+    for kind, text in _OUTCOME_TEXT.items():
+        if message.startswith(text):
+            return kind
+    raise ValueError(f"unknown outcome: {message}")
+
+
+def oracle_outcome(oracle, model):
+    """How the oracle's solve of ``model`` ends: "mechanism", "nonfinite_diag",
+    "rho_initial", "not_spd", "rho", "maxit" or "converged" (then with its output)."""
+    try:
+        out = oracle.solve_model(model.copy())
+    except RuntimeError as err:
+        if "mechanism" in str(err):
+            return "mechanism", None
+        if "PCG setup" in str(err):  # the oracle's Jacobi setup threw on a non-finite diagonal
+            return "nonfinite_diag", None
+        raise
+    rep = out["report"]
+    if rep["status"]:
+        return _ORACLE_STATUS[int(rep["status"])], None
+    return ("converged" if rep["converged"] else "maxit"), out
+
+
 CASES = {"single_q4": single_q4, "scrambled": scrambled, "grid6": grid6, "beam": beam, "strain": strain}
 
 # (storage, preconditioner, subdomain_split, subdomain_nodes) of each golden variant

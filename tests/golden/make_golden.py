@@ -18,6 +18,8 @@ Cases:
   beam       24x12 perturbed two-material beam: gravity + top pressure, colouring
   strain     16x8 plane-strain cantilever with RCM (the 1000x1000 workload's physics)
   adjoint    20x20 cantilever with log-normal per-element moduli + reference FD
+  failures   degenerate inputs (NaN/inf/negative moduli, NaN/inf loads, a floating
+             node): how the public solve() ends for each preconditioner and storage
   cfg1       the 200x200 workload: iteration counts, residuals, sampled u and R
   cfg2       the 1000x1000 workload: known answers from the reference.  These runs
              take hours; `--run-cfg2 DIR` makes them (ref_dump output per variant
@@ -111,6 +113,34 @@ CFG2_VARIANTS = {
 }
 
 
+def failure_outcomes() -> tuple[dict, dict]:
+    """How the reference's public solve() ends on each model of FAILURE_MODELS
+    (tests/cases.py), for every preconditioner and storage.  Non-finite moduli and
+    loads cannot pass the parser, so they go in as ref_dump overrides after
+    parsing, with validation off (the solver needs only an indexed model)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from cases import FAILURE_MODELS
+    outcomes, arrays = {}, {}
+    for name, make in FAILURE_MODELS.items():
+        model = make()
+        overrides = []
+        for k in np.flatnonzero(~np.isfinite(model.young)):
+            overrides.append(f"set_young={int(model.material_ids[k])}:{float(model.young[k])!r}")
+            model.young[k] = 1.0e6
+        for k in np.flatnonzero(~np.isfinite(model.load_fy)):
+            overrides.append(f"set_fy={int(model.load_node[k])}:{float(model.load_fy[k])!r}")
+            model.load_fy[k] = 0.0
+        outcomes[name] = {}
+        for precond in ("jacobi", "block", "ic0"):
+            for storage in ("csr", "bsr"):
+                va, vr = run(model, "outcome=1", "validate=0", f"storage={storage}", f"preconditioner={precond}",
+                             "subdomain_split=chunk", "subdomain_nodes=1", *overrides)
+                outcomes[name][f"{storage}_{precond}"] = vr
+                if "u" in va:
+                    arrays[f"{name}__{storage}_{precond}"] = va["u"]
+    return outcomes, arrays
+
+
 def save(name: str, arrays: dict) -> None:
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **arrays)
 
@@ -120,9 +150,19 @@ def main() -> None:
     ap = argparse.ArgumentParser(description="regenerate tests/golden from the reference's sources")
     ap.add_argument("--cfg2-dir", help="read the 1000x1000 reference runs from this directory")
     ap.add_argument("--run-cfg2", help="make the 1000x1000 reference runs in this directory (hours)")
+    ap.add_argument("--failures-only", action="store_true",
+                    help="remake only the failure-detection outcomes; keep every other fixture")
     args = ap.parse_args()
     if not os.path.exists(REF_DUMP):
         raise SystemExit("build the reference first: make -C oracle ref")
+    if args.failures_only:
+        with open(os.path.join(OUT, "golden.json")) as fh:
+            golden = json.load(fh)
+        golden["failures"], arrays = failure_outcomes()
+        save("failures", arrays)
+        with open(os.path.join(OUT, "golden.json"), "w") as fh:
+            json.dump(golden, fh, indent=1, sort_keys=True)
+        return
     golden: dict = {}
 
     # --- single Q4 and scrambled mesh: every stage, serial and colouring assembly
@@ -204,6 +244,10 @@ def main() -> None:
     report["tip_node"] = tip
     golden["adjoint"] = report
     save("adjoint", arrays)
+
+    # --- failure detection: how the public solve() ends on degenerate inputs
+    golden["failures"], arrays = failure_outcomes()
+    save("failures", arrays)
 
     # --- the 200x200 workload: iteration counts and sampled fields
     model = mesh.workload(1)

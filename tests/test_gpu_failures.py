@@ -1,0 +1,71 @@
+"""Failure detection of the CUDA path against the reference.
+
+Each of FAILURE_MODELS (tests/cases.py) makes the reference's public solve()
+stop, or finish, in one known way: the zero-pivot sweep (src/solver.cpp:920-940),
+the Jacobi setup (inverse_diagonal_of, :656-669), the three checks of pcg_solve
+(:579-581, :591-593, :616-618) or the "initial residual satisfies tolerance" exit
+(:573-578, where sqrt(max(0, NaN)) is 0).  The "failures" entry of golden.json
+and tests/golden/failures.npz hold how the reference ended on each; the GPU solve
+must end the same way.  Every failure here is a status the kernels set and the
+host reads after the launch: none of these cases faults, traps or hangs the GPU.
+"""
+
+import numpy as np
+import pytest
+
+from cases import FAILURE_DETERMINISTIC, FAILURE_MODELS, by_id_order, failure_case, outcome_kind
+from conftest import load_golden
+from lightfem_gb300.solver import LinearElasticSolver
+
+pytestmark = pytest.mark.gpu
+
+_PCG_KINDS = ("rho_initial", "not_spd", "rho")
+
+
+def gpu_outcome(model, precision="fp64"):
+    """How LinearElasticSolver.solve ends: "converged" (with the result) or the
+    kind of the reference exception its message carries."""
+    model.settings.precision = precision
+    try:
+        return "converged", LinearElasticSolver().solve(model)
+    except RuntimeError as err:
+        if str(err).startswith("PCG did not converge"):
+            return "maxit", None
+        return outcome_kind(str(err)), None
+
+
+@pytest.mark.parametrize("storage", ["csr", "bsr"])
+@pytest.mark.parametrize("precond", ["jacobi", "block", "ic0"])
+@pytest.mark.parametrize("name", list(FAILURE_MODELS))
+def test_fp64_failure_matches_reference(native, golden_json, name, precond, storage):
+    ref = golden_json["failures"][name][f"{storage}_{precond}"]
+    want = outcome_kind(ref["outcome"])
+    model = failure_case(name, storage, precond)
+    got, res = gpu_outcome(model)
+    assert got == want
+    if want != "converged":
+        return
+    assert abs(res.solver.iterations - ref["iterations"]) <= 2
+    u_ref = load_golden("failures")[f"{name}__{storage}_{precond}"]
+    u = by_id_order(model, res.displacement)
+    assert np.linalg.norm(u - u_ref) <= 1e-8 * np.linalg.norm(u_ref) or np.array_equal(u, u_ref)
+
+
+@pytest.mark.parametrize("storage", ["csr", "bsr"])
+@pytest.mark.parametrize("precond", ["jacobi", "block"])
+@pytest.mark.parametrize("name", list(FAILURE_MODELS))
+def test_mixed_failure_matches_reference(native, golden_json, name, precond, storage):
+    """The FP32-inner solve ends as the FP64 reference does where the outcome is
+    fixed at the start.  On an indefinite K (negative modulus) where breakdown comes
+    later, it must either break down with one of pcg_solve's errors or reach the
+    FP64 target on the true residual."""
+    want = outcome_kind(golden_json["failures"][name][f"{storage}_{precond}"]["outcome"])
+    model = failure_case(name, storage, precond)
+    got, res = gpu_outcome(model, precision="mixed")
+    if name in FAILURE_DETERMINISTIC or want == "converged":
+        assert got == want
+    else:
+        assert got in ("converged", *_PCG_KINDS)
+    if got == "converged" and np.all(np.isfinite(model.load_fy)):
+        target = model.settings.tolerance * max(1.0, res.solver.initial_residual)
+        assert res.solver.true_residual <= 1.2 * target

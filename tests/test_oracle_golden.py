@@ -7,7 +7,8 @@ applications are compared at rounding level.  CPU only."""
 import numpy as np
 import pytest
 
-from cases import CASES, VARIANTS, adjoint_model, by_id_order, indexed
+from cases import (CASES, FAILURE_MODELS, VARIANTS, adjoint_model, by_id_order, failure_case, indexed,
+                   oracle_outcome, outcome_kind)
 from conftest import load_golden
 from lightfem_gb300 import mesh
 
@@ -193,3 +194,20 @@ def test_postprocess_matches_reference(oracle, name):
     fields, nodal = oracle.postprocess(model.xy, en, model.young[mi], model.poisson[mi], model.settings.plane_mode, u)
     np.testing.assert_array_equal(fields, g["post_fields"])
     np.testing.assert_array_equal(nodal, g["post_nodal"])
+
+
+@pytest.mark.parametrize("name", list(FAILURE_MODELS))
+def test_failure_outcomes_match_reference(oracle, golden_json, name):
+    """Degenerate inputs (NaN / inf / negative moduli, NaN / inf loads, a node in no
+    element) end the oracle's solve exactly as they end the reference's public
+    solve(): the same exception, or convergence after the same iterations to the
+    same displacements."""
+    g = load_golden("failures")
+    for variant, ref in golden_json["failures"][name].items():
+        storage, precond = variant.split("_")
+        model = failure_case(name, storage, precond)
+        kind, out = oracle_outcome(oracle, model)
+        assert kind == outcome_kind(ref["outcome"]), variant
+        if kind == "converged":
+            assert out["report"]["iterations"] == ref["iterations"], variant
+            np.testing.assert_array_equal(by_id_order(model, out["u"]), g[f"{name}__{variant}"])
