@@ -68,7 +68,11 @@ typedef enum lfgpu_status {
 enum { LFGPU_PLANE_STRESS = 0, LFGPU_PLANE_STRAIN = 1 };
 enum { LFGPU_ASSEMBLY_COLORING = 0, LFGPU_ASSEMBLY_ATOMIC = 1 };
 enum { LFGPU_STORAGE_CSR = 0, LFGPU_STORAGE_BSR = 1 };
-enum { LFGPU_PRECOND_JACOBI = 0, LFGPU_PRECOND_BLOCK2 = 1, LFGPU_PRECOND_IC0 = 2 };
+/* BLOCK2: the 2x2 nodal case (subdomain_nodes 1) fused into the loop kernels.
+ * SUBDOMAIN: SubdomainBlockJacobi with the handle's lfgpu_set_subdomains split
+ * (the reference's `preconditioner block` with any subdomain_nodes); FP64 only. */
+enum { LFGPU_PRECOND_JACOBI = 0, LFGPU_PRECOND_BLOCK2 = 1, LFGPU_PRECOND_IC0 = 2, LFGPU_PRECOND_SUBDOMAIN = 3 };
+enum { LFGPU_SPLIT_RCB = 0, LFGPU_SPLIT_CHUNK = 1 };
 enum { LFGPU_PRECISION_FP64 = 0, LFGPU_PRECISION_MIXED = 1 };
 enum { LFGPU_REFINE_RELIABLE = 0, LFGPU_REFINE_RESTART = 1 };
 enum { LFGPU_EDGE_TRACTION = 0, LFGPU_EDGE_PRESSURE = 1 };
@@ -115,9 +119,9 @@ typedef struct lfgpu_report {
     double storage_convert_ms;
     double preconditioner_setup_ms;
     double preconditioner_apply_ms;  /* IC0 only: device time of the triangular sweeps */
-    int64_t subdomains;              /* block: number of 2x2 nodal blocks */
-    double capture_ratio;            /* block: share of nonzeros inside a subdomain */
-    int64_t degenerate_subdomains;   /* block: blocks that fell back to the identity */
+    int64_t subdomains;              /* block / subdomain: number of subdomains (2x2 nodal blocks for block) */
+    double capture_ratio;            /* block / subdomain: share of nonzeros inside a subdomain */
+    int64_t degenerate_subdomains;   /* block / subdomain: blocks that fell back to the identity */
     int64_t ic0_breakdowns;          /* ic0: clamped pivots */
     int64_t ic0_levels;              /* ic0: forward + backward level count */
     int64_t fallback_fp64;           /* mixed: 1 if the FP32 inner solve stagnated and FP64 PCG finished */
@@ -222,9 +226,21 @@ int lfgpu_event_elapsed(lfgpu_t h, int32_t slot_a, int32_t slot_b, double* ms);
 int lfgpu_spmv(lfgpu_t h, int32_t which, int32_t storage, int32_t precision, const double* x,
                double* y, int32_t repeat, double* ms_per_call);
 
+/* Subdomains of the SUBDOMAIN preconditioner (build_dof_subdomain,
+ * src/solver.cpp:631-653): nodes_per_subdomain nodes each, split LFGPU_SPLIT_RCB
+ * (split_by_coordinates, src/precond.cpp:30-105) or LFGPU_SPLIT_CHUNK
+ * (split_by_chunks, :19-28) over the node order of lfgpu_set_mesh.  The defaults
+ * are the reference's (64, RCB; include/lightfem/model.hpp:107-108).  RCB pieces
+ * can hold up to about twice the requested nodes.  One CTA factors and solves a
+ * subdomain, a thread per DOF, so a subdomain holds at most
+ * LFGPU_SUBDOMAIN_MAX_DOFS DOFs; a larger one makes the solve return
+ * LFGPU_ERR_UNSUPPORTED. */
+#define LFGPU_SUBDOMAIN_MAX_DOFS 1024
+int lfgpu_set_subdomains(lfgpu_t h, int64_t nodes_per_subdomain, int32_t split);
+
 /* One FP64 application z = M^-1 r of a preconditioner of K_CONSTRAINED, built on
  * first use: JacobiPreconditioner::apply (src/solver.cpp:497-509), the 2x2 nodal
- * SubdomainBlockJacobi::apply (src/precond.cpp:242-291) or
+ * or the general SubdomainBlockJacobi::apply (src/precond.cpp:242-291) or
  * IncompleteCholesky0::apply (src/precond.cpp:386-412).  *ms (may be NULL) gets the
  * device time of the application. */
 int lfgpu_apply_preconditioner(lfgpu_t h, int32_t preconditioner, const double* r, double* z,
@@ -274,6 +290,11 @@ int lfgpu_mesh_profile(lfgpu_t h, int64_t* profile_out);
 /* reverse_cuthill_mckee (src/reordering.cpp:11-62): node IDs in the new order. */
 int lfgpu_host_rcm(int64_t n_nodes, const int64_t* node_ids, int64_t n_elements,
                    const int64_t* element_node_ids, int64_t* order_out);
+/* split_by_chunks / split_by_coordinates (src/precond.cpp:19-105): subdomain of
+ * every node (owner_out[n_nodes]) and the subdomain count; xy holds 2 coordinates
+ * per node.  The split lfgpu_set_subdomains uses. */
+int lfgpu_host_subdomains(int64_t n_nodes, const double* xy, int64_t nodes_per_subdomain, int32_t split,
+                          uint32_t* owner_out, int64_t* count_out);
 
 #ifdef __cplusplus
 }

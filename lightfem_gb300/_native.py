@@ -23,7 +23,9 @@ ERR_SCRATCH_LIMIT = 14
 NOALLOC_MAX_ROWS = 4194304  # LFGPU_NOALLOC_MAX_ROWS
 ASSEMBLY = {"coloring": 0, "atomic": 1}
 STORAGE = {"csr": 0, "bsr": 1}
-PRECOND = {"jacobi": 0, "block": 1, "ic0": 2}
+PRECOND = {"jacobi": 0, "block": 1, "ic0": 2, "subdomain": 3}  # block: 2x2 nodal; subdomain: any size
+SPLIT = {"rcb": 0, "chunk": 1}
+SUBDOMAIN_MAX_DOFS = 1024  # LFGPU_SUBDOMAIN_MAX_DOFS
 PRECISION = {"fp64": 0, "mixed": 1}
 REFINEMENT = {"reliable": 0, "restart": 1}
 K_FULL, K_CONSTRAINED, F_FULL, F_CONSTRAINED, U, R = range(6)
@@ -102,7 +104,9 @@ _SIGNATURES = {
     "lfgpu_apply_preconditioner": (c_int, [c_void_p, c_int32, c_void_p, c_void_p, POINTER(c_double)]),
     "lfgpu_residual_norm_noalloc": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                             POINTER(c_double)]),
+    "lfgpu_set_subdomains": (c_int, [c_void_p, c_int64, c_int32]),
     "lfgpu_host_rcm": (c_int, [c_int64, c_void_p, c_int64, c_void_p, c_void_p]),
+    "lfgpu_host_subdomains": (c_int, [c_int64, c_void_p, c_int64, c_int32, c_void_p, POINTER(c_int64)]),
 }
 
 EXPORTED = tuple(_SIGNATURES)
@@ -141,6 +145,19 @@ def host_rcm(node_ids: np.ndarray, element_node_ids: np.ndarray) -> np.ndarray:
     if rc != OK:
         raise GpuError(rc, "RCM ordering failed: element references an unknown node ID")
     return out
+
+
+def host_subdomains(xy: np.ndarray, nodes_per_subdomain: int, split: str = "rcb") -> tuple[np.ndarray, int]:
+    """split_by_coordinates / split_by_chunks (src/precond.cpp:19-105): the
+    subdomain of every node (node index order) and the subdomain count."""
+    pts = _arr(xy, np.float64).reshape(-1, 2)
+    owner = np.empty(pts.shape[0], np.uint32)
+    count = c_int64()
+    rc = library().lfgpu_host_subdomains(pts.shape[0], _ptr(pts), int(nodes_per_subdomain), SPLIT[split],
+                                         _ptr(owner), ctypes.byref(count))
+    if rc != OK:
+        raise GpuError(rc, f"subdomain split failed with status {rc}")
+    return owner, int(count.value)
 
 
 def residual_norm_noalloc(n_rows: int, row_offsets: int, columns: int, values: int, u: int, f: int,
@@ -339,6 +356,10 @@ class Context:
         nodal = np.empty((self.n_dofs // 2, 4))
         self._check(self._lib.lfgpu_postprocess(self._h, _ptr(fields), _ptr(nodal)))
         return fields, nodal
+
+    def set_subdomains(self, nodes_per_subdomain: int = 64, split: str = "rcb") -> None:
+        """The split of the "subdomain" preconditioner (subdomain_nodes, subdomain_split)."""
+        self._check(self._lib.lfgpu_set_subdomains(self._h, int(nodes_per_subdomain), SPLIT[split]))
 
     def apply_preconditioner(self, r, preconditioner: str = "jacobi"):
         """z = M^-1 r for the constrained K; returns (z, device ms)."""

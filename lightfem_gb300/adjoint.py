@@ -25,7 +25,7 @@ import torch
 
 from . import _native
 from .model import Model
-from .solver import upload_model
+from .solver import gpu_preconditioner, upload_model
 
 
 class ElasticProblem:
@@ -58,15 +58,18 @@ class ElasticProblem:
         self.strategy = "atomic" if s.assembly == "atomic" or s.gpu_assembly == "atomic" else "coloring"
         tol = tolerance if tolerance is not None else s.tolerance
         maxit = max_iterations if max_iterations is not None else s.max_iterations
-        self.options = _native.Context.options(tol, maxit, storage or s.storage, preconditioner or s.preconditioner,
+        precond = preconditioner or gpu_preconditioner(s)
+        self.options = _native.Context.options(tol, maxit, storage or s.storage, precond,
                                                precision or s.precision, s.refinement)
         self.adjoint_options = _native.Context.options(
             adjoint_tolerance if adjoint_tolerance is not None else tol, maxit, storage or s.storage,
-            preconditioner or s.preconditioner, precision or s.precision, s.refinement)
+            precond, precision or s.precision, s.refinement)
         _, values = m.constraints()
         self.homogeneous_supports = bool(np.all(np.asarray(values) == 0.0))
         self.ctx = _native.Context(device)
         upload_model(self.ctx, m)
+        if precond == "subdomain":
+            self.ctx.set_subdomains(s.subdomain_nodes, s.subdomain_split)
         self._solved_for: np.ndarray | None = None
         self.report = None
         self.adjoint_report = None

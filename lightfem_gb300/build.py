@@ -19,7 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "liblfgpu.so")
 
-CUDA_SOURCES = ["api.cu", "assemble.cu", "sparse.cu", "pcg.cu", "cg_graph.cu", "ic0.cu", "adjoint.cu", "noalloc.cu", "pattern.cu", "postprocess.cu"]
+CUDA_SOURCES = ["api.cu", "assemble.cu", "sparse.cu", "pcg.cu", "cg_graph.cu", "ic0.cu", "adjoint.cu", "noalloc.cu",
+                "pattern.cu", "postprocess.cu", "subdomain.cu"]
 HOST_SOURCES = ["host_setup.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -555,12 +555,12 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
         LF_REQUIRE(o->max_iterations > 0, LFGPU_ERR_ARGUMENT, "max_iterations must be greater than zero");
         LF_REQUIRE(o->storage == LFGPU_STORAGE_CSR || o->storage == LFGPU_STORAGE_BSR, LFGPU_ERR_ARGUMENT,
                    "storage must be csr or bsr");
-        LF_REQUIRE(o->preconditioner >= LFGPU_PRECOND_JACOBI && o->preconditioner <= LFGPU_PRECOND_IC0,
-                   LFGPU_ERR_ARGUMENT, "preconditioner must be jacobi, block or ic0");
+        LF_REQUIRE(o->preconditioner >= LFGPU_PRECOND_JACOBI && o->preconditioner <= LFGPU_PRECOND_SUBDOMAIN,
+                   LFGPU_ERR_ARGUMENT, "preconditioner must be jacobi, block, ic0 or subdomain");
         LF_REQUIRE(o->precision == LFGPU_PRECISION_FP64 || o->precision == LFGPU_PRECISION_MIXED, LFGPU_ERR_ARGUMENT,
                    "precision must be fp64 or mixed");
-        LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner == LFGPU_PRECOND_IC0),
-                   LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi and block preconditioners");
+        LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner >= LFGPU_PRECOND_IC0),
+                   LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi and 2x2 block preconditioners");
         lfgpu_report r{};
         r.status = LFGPU_OK;
         const double fnorm = device_norm2(*h, h->f, h->n);
@@ -590,10 +590,21 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
             LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
             r.preconditioner_setup_ms = elapsed_ms(*h);
             if (o->storage == LFGPU_STORAGE_BSR) ensure_bsr(*h);
-            res = run_pcg_ic0(*h, s, &ms, &apply_ms);
+            res = run_pcg_separate(*h, s, &ms, &apply_ms);
             r.ic0_breakdowns = h->ic0_breakdowns;
             r.ic0_levels = h->ic0_levels;
             r.preconditioner_apply_ms = apply_ms;
+        } else if (o->preconditioner == LFGPU_PRECOND_SUBDOMAIN) {
+            LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
+            ensure_subdomains(*h);
+            LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
+            r.preconditioner_setup_ms = elapsed_ms(*h);
+            if (o->storage == LFGPU_STORAGE_BSR) ensure_bsr(*h);
+            res = run_pcg_separate(*h, s, &ms, &apply_ms);
+            r.preconditioner_apply_ms = apply_ms;
+            r.subdomains = h->sub_count;
+            r.capture_ratio = h->sub_capture;
+            r.degenerate_subdomains = h->sub_degenerate;
         } else {
             LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
             ensure_preconditioners(*h, o->preconditioner);
@@ -815,8 +826,8 @@ int lfgpu_postprocess(lfgpu_t h, double* element_fields, double* nodal_stress) {
 int lfgpu_apply_preconditioner(lfgpu_t h, int32_t preconditioner, const double* r, double* z, double* ms) {
     return guarded(h, [&] {
         LF_REQUIRE(h->constrained, LFGPU_ERR_STATE, "apply boundary conditions before preconditioning");
-        LF_REQUIRE(preconditioner >= LFGPU_PRECOND_JACOBI && preconditioner <= LFGPU_PRECOND_IC0, LFGPU_ERR_ARGUMENT,
-                   "preconditioner must be jacobi, block or ic0");
+        LF_REQUIRE(preconditioner >= LFGPU_PRECOND_JACOBI && preconditioner <= LFGPU_PRECOND_SUBDOMAIN,
+                   LFGPU_ERR_ARGUMENT, "preconditioner must be jacobi, block, ic0 or subdomain");
         LF_REQUIRE(r != nullptr && z != nullptr, LFGPU_ERR_ARGUMENT, "null vector");
         const i64 n = h->n;
         for (auto& b : h->v64) b.ensure(n);
@@ -824,6 +835,7 @@ int lfgpu_apply_preconditioner(lfgpu_t h, int32_t preconditioner, const double* 
         Buf<double>& zd = h->v64[3];
         LF_CUDA(cudaMemcpyAsync(rd.p, r, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
         if (preconditioner == LFGPU_PRECOND_IC0) ensure_ic0(*h);
+        else if (preconditioner == LFGPU_PRECOND_SUBDOMAIN) ensure_subdomains(*h);
         else ensure_preconditioners(*h, preconditioner);
         LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
         launch_precond_apply(*h, preconditioner, rd, zd);
@@ -850,8 +862,10 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
             LF_CUDA(cudaMemcpyAsync(lam.p, h->u.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
         } else {
             LF_REQUIRE(o != nullptr, LFGPU_ERR_ARGUMENT, "the adjoint solve needs solve options");
-            LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner == LFGPU_PRECOND_IC0),
-                       LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi and block preconditioners");
+            LF_REQUIRE(o->preconditioner >= LFGPU_PRECOND_JACOBI && o->preconditioner <= LFGPU_PRECOND_SUBDOMAIN,
+                       LFGPU_ERR_ARGUMENT, "preconditioner must be jacobi, block, ic0 or subdomain");
+            LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner >= LFGPU_PRECOND_IC0),
+                       LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi and 2x2 block preconditioners");
             // Solve K lambda = dJ/du with dJ/du zeroed on the constrained DOFs: reuse the
             // solve machinery on the adjoint right-hand side.
             std::vector<double> rhs(dj_du, dj_du + n);
@@ -882,9 +896,10 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
             float ms = 0.f;
             double apply_ms = 0.0;
             PcgResult res;
-            if (o->preconditioner == LFGPU_PRECOND_IC0) {
-                ensure_ic0(*h);
-                res = run_pcg_ic0(*h, s, &ms, &apply_ms);
+            if (o->preconditioner == LFGPU_PRECOND_IC0 || o->preconditioner == LFGPU_PRECOND_SUBDOMAIN) {
+                if (o->preconditioner == LFGPU_PRECOND_IC0) ensure_ic0(*h);
+                else ensure_subdomains(*h);
+                res = run_pcg_separate(*h, s, &ms, &apply_ms);
             } else {
                 ensure_preconditioners(*h, o->preconditioner);
                 res = o->persistent ? run_pcg(*h, s, &ms) : run_cg_graph(*h, s, &ms);
@@ -960,6 +975,31 @@ int lfgpu_rcm(lfgpu_t h, int64_t* order_out) {
         }
         h->timings.rcm_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     });
+}
+
+int lfgpu_set_subdomains(lfgpu_t h, int64_t nodes_per_subdomain, int32_t split) {
+    return guarded(h, [&] {
+        LF_REQUIRE(nodes_per_subdomain >= 1, LFGPU_ERR_ARGUMENT, "subdomain_nodes must be at least 1");
+        LF_REQUIRE(split == LFGPU_SPLIT_RCB || split == LFGPU_SPLIT_CHUNK, LFGPU_ERR_ARGUMENT,
+                   "subdomain_split must be rcb or chunk");
+        h->sub_nodes = nodes_per_subdomain;
+        h->sub_split = split;
+    });
+}
+
+int lfgpu_host_subdomains(int64_t n_nodes, const double* xy, int64_t nodes_per_subdomain, int32_t split,
+                          uint32_t* owner_out, int64_t* count_out) {
+    if (n_nodes < 0 || nodes_per_subdomain < 1 || (split != LFGPU_SPLIT_RCB && split != LFGPU_SPLIT_CHUNK) ||
+        !count_out || (n_nodes > 0 && (!xy || !owner_out)))
+        return LFGPU_ERR_ARGUMENT;
+    try {
+        std::vector<uint32_t> owner;
+        *count_out = subdomain_split(n_nodes, xy, nodes_per_subdomain, split == LFGPU_SPLIT_RCB, owner);
+        std::copy(owner.begin(), owner.end(), owner_out);
+    } catch (...) {
+        return LFGPU_ERR_NOMEM;
+    }
+    return LFGPU_OK;
 }
 
 int lfgpu_host_rcm(int64_t n_nodes, const int64_t* node_ids, int64_t n_elements, const int64_t* element_node_ids,

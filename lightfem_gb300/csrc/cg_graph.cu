@@ -79,6 +79,10 @@ struct CgArgs {
     const double* icinv;           // IC(0) reciprocal pivots
     double* y;                     // IC(0) forward-sweep result
     unsigned long long* ic_chunks; // IC(0) row-chunk counters (forward, backward)
+    const int* sub_dofs;           // subdomain block-Jacobi: DOFs by subdomain
+    const int* sub_begin;
+    const long long* sub_fac;      // packed lower factor offset of each subdomain
+    const double* sub_factor;
     int blocks;
     CgState* st;
     DeviceStatus* status;
@@ -879,13 +883,14 @@ __global__ void __launch_bounds__(kSweepRows) ic0_backward(CgArgs a) {
 }
 
 __device__ __forceinline__ void ic0_mark_pending(const CgArgs& a, int i) {
+    if (a.y == nullptr) return;  // the subdomain preconditioner writes z without polls
     const double pending = __longlong_as_double(static_cast<long long>(kPending));
     reinterpret_cast<double2*>(a.y)[i] = make_double2(pending, pending);
     reinterpret_cast<double2*>(a.z)[i] = make_double2(pending, pending);
 }
 
 __device__ __forceinline__ void ic0_reset_chunks(const CgArgs& a) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (a.ic_chunks != nullptr && blockIdx.x == 0 && threadIdx.x == 0) {
         a.ic_chunks[0] = 0ull;
         a.ic_chunks[1] = 0ull;
     }
@@ -996,6 +1001,38 @@ __global__ void __launch_bounds__(kThreads) ic0_dot(CgArgs a) {
         }
         set_loop(a, !s->done);
     });
+}
+
+// One application z = M^-1 r of the subdomain block-Jacobi preconditioner
+// (SubdomainBlockJacobi::apply, src/precond.cpp:242-282): one CTA per subdomain,
+// thread i holding local row i.  Forward substitution with the packed lower
+// factor, then back substitution with its transpose, column by column: after
+// unknown j is final every later row subtracts its term, so each row subtracts
+// its terms in the reference's order (ascending forward, descending backward),
+// each product and difference rounded on its own.  The result equals the
+// reference's bit for bit.
+__global__ void __launch_bounds__(LFGPU_SUBDOMAIN_MAX_DOFS) subdomain_apply(CgArgs a) {
+    __shared__ double v[LFGPU_SUBDOMAIN_MAX_DOFS];
+    const int s = blockIdx.x, i = threadIdx.x;
+    const int begin = a.sub_begin[s], D = a.sub_begin[s + 1] - begin;
+    const double* f = a.sub_factor + a.sub_fac[s];
+    const bool mine = i < D;
+    const int dof = mine ? a.sub_dofs[begin + i] : 0;
+    const double* row = f + static_cast<long long>(i) * (i + 1) / 2;  // this thread's factor row
+    double acc = mine ? a.r[dof] : 0.0;
+    for (int j = 0; j < D; ++j) {
+        if (i == j) v[j] = __dmul_rn(acc, row[j]);  // row[j] is the reciprocal pivot
+        __syncthreads();
+        if (mine && i > j) acc = __dsub_rn(acc, __dmul_rn(row[j], v[j]));
+    }
+    acc = mine ? v[i] : 0.0;
+    double x = 0.0;
+    for (int k = D - 1; k >= 0; --k) {
+        if (i == k) v[k] = x = __dmul_rn(acc, row[k]);
+        __syncthreads();
+        if (i < k) acc = __dsub_rn(acc, __dmul_rn(f[static_cast<long long>(k) * (k + 1) / 2 + i], v[k]));
+    }
+    if (mine) a.z[dof] = x;
 }
 
 // One FP64 application of the Jacobi or 2x2 nodal preconditioner.
@@ -1150,49 +1187,76 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
 
 // IC(0): init -> forward -> backward -> start -> WHILE { product ; update ;
 // forward ; backward ; dot ; p update }.  The sweeps run one CTA per row chunk.
-template <int STORAGE>
-void build_ic0(cudaGraph_t g, CgArgs* a, int blocks, int chunks) {
-    cudaGraphNode_t n_res = nullptr, n_init, n_fwd, n_bwd, n_start;
-    if (a->x0) add_kernel(g, &n_res, nullptr, 0, cg64_residual<STORAGE>, blocks, a);
-    add_kernel(g, &n_init, a->x0 ? &n_res : nullptr, a->x0 ? 1 : 0, ic0_init, blocks, a);
-    add_kernel(g, &n_fwd, &n_init, 1, ic0_forward, chunks, a, 0, kSweepRows);
-    add_kernel(g, &n_bwd, &n_fwd, 1, ic0_backward, chunks, a, 0, kSweepRows);
-    add_kernel(g, &n_start, &n_bwd, 1, ic0_start, blocks, a);
-    cudaGraph_t body;
-    add_conditional(g, &n_start, 1, a->loop, cudaGraphCondTypeWhile, &body);
-    cudaGraphNode_t k[6];
-    add_kernel(body, &k[0], nullptr, 0, cg64_product<STORAGE>, blocks, a);
-    add_kernel(body, &k[1], &k[0], 1, ic0_update, blocks, a);
-    add_kernel(body, &k[2], &k[1], 1, ic0_forward, chunks, a, 0, kSweepRows);
-    add_kernel(body, &k[3], &k[2], 1, ic0_backward, chunks, a, 0, kSweepRows);
-    add_kernel(body, &k[4], &k[3], 1, ic0_dot, blocks, a);
-    add_kernel(body, &k[5], &k[4], 1, cg64_direction, blocks, a);
+// The subdomain block-Jacobi form is the same with one apply kernel (one CTA per
+// subdomain) in place of the two sweeps.
+struct SeparateApply {
+    bool subdomain;
+    int chunks;    // IC(0): row chunks of the sweeps
+    int sub_grid;  // subdomain: subdomains, and threads per CTA
+    int sub_threads;
+};
+
+// Adds the application after `dep`; returns its last node.
+cudaGraphNode_t add_apply(cudaGraph_t g, cudaGraphNode_t dep, CgArgs* a, const SeparateApply& ap) {
+    cudaGraphNode_t n1, n2;
+    if (ap.subdomain) {
+        add_kernel(g, &n1, &dep, 1, subdomain_apply, ap.sub_grid, a, 0, ap.sub_threads);
+        return n1;
+    }
+    add_kernel(g, &n1, &dep, 1, ic0_forward, ap.chunks, a, 0, kSweepRows);
+    add_kernel(g, &n2, &n1, 1, ic0_backward, ap.chunks, a, 0, kSweepRows);
+    return n2;
 }
 
-// Phase slots: 0 product, 1 update, 2 forward sweep, 3 backward sweep, 4 r.z,
-// 5 p update.
 template <int STORAGE>
-void launch_ic0_unrolled(cudaStream_t stream, CgArgs* a, int blocks, int chunks, int iters, EventTrail& trail) {
+void build_separate(cudaGraph_t g, CgArgs* a, int blocks, const SeparateApply& ap) {
+    cudaGraphNode_t n_res = nullptr, n_init, n_start;
+    if (a->x0) add_kernel(g, &n_res, nullptr, 0, cg64_residual<STORAGE>, blocks, a);
+    add_kernel(g, &n_init, a->x0 ? &n_res : nullptr, a->x0 ? 1 : 0, ic0_init, blocks, a);
+    const cudaGraphNode_t n_apply = add_apply(g, n_init, a, ap);
+    add_kernel(g, &n_start, &n_apply, 1, ic0_start, blocks, a);
+    cudaGraph_t body;
+    add_conditional(g, &n_start, 1, a->loop, cudaGraphCondTypeWhile, &body);
+    cudaGraphNode_t k[4];
+    add_kernel(body, &k[0], nullptr, 0, cg64_product<STORAGE>, blocks, a);
+    add_kernel(body, &k[1], &k[0], 1, ic0_update, blocks, a);
+    const cudaGraphNode_t k_apply = add_apply(body, k[1], a, ap);
+    add_kernel(body, &k[2], &k_apply, 1, ic0_dot, blocks, a);
+    add_kernel(body, &k[3], &k[2], 1, cg64_direction, blocks, a);
+}
+
+// Phase slots: 0 product, 1 update, 2 forward sweep (subdomain: the block
+// solves), 3 backward sweep, 4 r.z, 5 p update.
+template <int STORAGE>
+void launch_separate_unrolled(cudaStream_t stream, CgArgs* a, int blocks, const SeparateApply& ap, int iters,
+                              EventTrail& trail) {
     auto chain = [&](auto kernel, int phase) {  // the loop kernels
         kernel<<<blocks, kThreads, 0, stream>>>(*a);
         LF_CUDA(cudaGetLastError());
         trail.mark(phase);
     };
-    auto sweep = [&](auto kernel, int phase) {  // one CTA per chunk of kSweepRows rows
-        kernel<<<chunks, kSweepRows, 0, stream>>>(*a);
+    auto apply = [&](bool in_loop) {
+        if (ap.subdomain) {
+            subdomain_apply<<<ap.sub_grid, ap.sub_threads, 0, stream>>>(*a);
+            LF_CUDA(cudaGetLastError());
+            trail.mark(in_loop ? 2 : -1);
+            return;
+        }
+        ic0_forward<<<ap.chunks, kSweepRows, 0, stream>>>(*a);  // one CTA per chunk of kSweepRows rows
         LF_CUDA(cudaGetLastError());
-        trail.mark(phase);
+        trail.mark(in_loop ? 2 : -1);
+        ic0_backward<<<ap.chunks, kSweepRows, 0, stream>>>(*a);
+        LF_CUDA(cudaGetLastError());
+        trail.mark(in_loop ? 3 : -1);
     };
     if (a->x0) chain(cg64_residual<STORAGE>, -1);
     chain(ic0_init, -1);
-    sweep(ic0_forward, -1);
-    sweep(ic0_backward, -1);
+    apply(false);
     chain(ic0_start, -1);
     for (int k = 0; k < iters; ++k) {
         chain(cg64_product<STORAGE>, 0);
         chain(ic0_update, 1);
-        sweep(ic0_forward, 2);
-        sweep(ic0_backward, 3);
+        apply(true);
         chain(ic0_dot, 4);
         chain(cg64_direction, 5);
     }
@@ -1317,9 +1381,12 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     // (FP64: product, update, direction; mixed: product, update) and per residual
     // replacement the two branch kernels; the profiling form launches every kernel
     // of every pass.
-    // IC(0): residual (warm start), init, two sweeps and start, then six kernels a pass.
+    // IC(0): residual (warm start), init, two sweeps and start, then six kernels a
+    // pass; subdomain block-Jacobi: one apply kernel in place of the two sweeps.
     if (s.precond == LFGPU_PRECOND_IC0)
         c.launches += (s.x0 ? 1 : 0) + 4 + 6 * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
+    else if (s.precond == LFGPU_PRECOND_SUBDOMAIN)
+        c.launches += (s.x0 ? 1 : 0) + 3 + 5 * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
     else if (s.unrolled > 0)
         c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 5 : 3) +
                       (s.mixed ? 1 : 0);
@@ -1350,14 +1417,29 @@ void ic0_args(Context& c, CgArgs& a) {
     a.ic_chunks = c.ic0_misc.p + kIc0ForwardChunk;
 }
 
+// The subdomain arrays, and the apply kernel's launch shape.
+SeparateApply subdomain_args(Context& c, CgArgs& a) {
+    a.sub_dofs = c.sub_dofs;
+    a.sub_begin = c.sub_begin;
+    a.sub_fac = c.sub_fac_begin;
+    a.sub_factor = c.sub_factor;
+    SeparateApply ap{};
+    ap.subdomain = true;
+    ap.sub_grid = static_cast<int>(c.sub_count);
+    ap.sub_threads = std::max(32, (c.sub_max + 31) / 32 * 32);
+    return ap;
+}
+
 }  // namespace
 
-PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double* apply_ms) {
+PcgResult run_pcg_separate(Context& c, const SolveSetup& s, float* kernel_ms, double* apply_ms) {
     const i64 n = c.n;
     LF_REQUIRE(n % 2 == 0, LFGPU_ERR_ARGUMENT, "the GPU PCG needs an even number of DOFs (u,v pairs)");
     LF_REQUIRE(!s.mixed, LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi and block preconditioners");
+    LF_REQUIRE(s.precond == LFGPU_PRECOND_IC0 || s.precond == LFGPU_PRECOND_SUBDOMAIN, LFGPU_ERR_ARGUMENT,
+               "separate-kernel preconditioners are ic0 and subdomain");
+    const bool sub = s.precond == LFGPU_PRECOND_SUBDOMAIN;
     const int blocks = c.num_sms * (2048 / kThreads);
-    const int chunks = static_cast<int>((n + kSweepRows - 1) / kSweepRows);
     CgArgs a{};
     a.n = static_cast<int>(n);
     a.nb = static_cast<int>(n / 2);
@@ -1372,14 +1454,20 @@ PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double*
     a.z = c.v64[1];
     a.p = c.v64[2];
     a.q = c.v64[3];
-    a.y = c.v64[4];
     if (s.storage == LFGPU_STORAGE_BSR) {
         ensure_bsr(c);
         a.brow = c.brow;
         a.bcol = c.bcol;
         a.bval64 = reinterpret_cast<const double2*>(c.bval64.p);
     }
-    ic0_args(c, a);
+    SeparateApply ap{};
+    if (sub) {
+        ap = subdomain_args(c, a);
+    } else {
+        a.y = c.v64[4];
+        ic0_args(c, a);
+        ap.chunks = static_cast<int>((n + kSweepRows - 1) / kSweepRows);
+    }
     c.partials.ensure(static_cast<size_t>(kSlots) * kMaxReduce * blocks);
     a.partials = c.partials;
     a.blocks = blocks;
@@ -1396,8 +1484,8 @@ PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double*
         LF_REQUIRE(s.unrolled <= 100000, LFGPU_ERR_ARGUMENT, "profiling runs are limited to 100000 passes");
         LF_CUDA(cudaEventRecord(c.ev_a, c.stream));
         EventTrail trail(c.stream, s.unrolled <= kTimedPasses);
-        if (csr) launch_ic0_unrolled<LFGPU_STORAGE_CSR>(c.stream, &a, blocks, chunks, s.unrolled, trail);
-        else launch_ic0_unrolled<LFGPU_STORAGE_BSR>(c.stream, &a, blocks, chunks, s.unrolled, trail);
+        if (csr) launch_separate_unrolled<LFGPU_STORAGE_CSR>(c.stream, &a, blocks, ap, s.unrolled, trail);
+        else launch_separate_unrolled<LFGPU_STORAGE_BSR>(c.stream, &a, blocks, ap, s.unrolled, trail);
         LF_CUDA(cudaEventRecord(c.ev_b, c.stream));
         *kernel_ms = elapsed_ms(c);
         trail.totals(phase_ns);
@@ -1405,8 +1493,8 @@ PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double*
         GraphBuilder gb{c};
         LF_CUDA(cudaGraphCreate(&gb.graph, 0));
         LF_CUDA(cudaGraphConditionalHandleCreate(&a.loop, gb.graph, 0, 0));
-        if (csr) build_ic0<LFGPU_STORAGE_CSR>(gb.graph, &a, blocks, chunks);
-        else build_ic0<LFGPU_STORAGE_BSR>(gb.graph, &a, blocks, chunks);
+        if (csr) build_separate<LFGPU_STORAGE_CSR>(gb.graph, &a, blocks, ap);
+        else build_separate<LFGPU_STORAGE_BSR>(gb.graph, &a, blocks, ap);
         cudaGraphExec_t exec = nullptr;
         LF_CUDA(cudaGraphInstantiate(&exec, gb.graph, 0));
         cudaError_t err = cudaEventRecord(c.ev_a, c.stream);
@@ -1418,10 +1506,10 @@ PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double*
     }
     PcgResult res = finish_cg(c, s);
     for (int k = 0; k < 6; ++k) res.phase_ns[k] = phase_ns[k];
-    // Time one standalone application (forward + backward sweep) on the final
-    // residual; the solve made iterations + 1 of them.
+    // Time one standalone application (forward + backward sweep, or the block
+    // solves) on the final residual; the solve made iterations + 1 of them.
     LF_CUDA(cudaEventRecord(c.ev_a, c.stream));
-    launch_precond_apply(c, LFGPU_PRECOND_IC0, c.v64[0], c.v64[5]);
+    launch_precond_apply(c, s.precond, c.v64[0], c.v64[5]);
     LF_CUDA(cudaEventRecord(c.ev_b, c.stream));
     const double one = elapsed_ms(c);
     check_status(c);
@@ -1458,6 +1546,10 @@ void launch_precond_apply(Context& c, int precond, const double* r, double* z) {
         ic0_forward<<<chunks, kSweepRows, 0, c.stream>>>(a);
         ic0_backward<<<chunks, kSweepRows, 0, c.stream>>>(a);
         c.launches += 2;
+    } else if (precond == LFGPU_PRECOND_SUBDOMAIN) {
+        const SeparateApply ap = subdomain_args(c, a);
+        if (ap.sub_grid > 0) subdomain_apply<<<ap.sub_grid, ap.sub_threads, 0, c.stream>>>(a);
+        c.launches += ap.sub_grid > 0 ? 1 : 0;
     } else if (precond == LFGPU_PRECOND_JACOBI) {
         precond_apply_kernel<LFGPU_PRECOND_JACOBI><<<blocks, kThreads, 0, c.stream>>>(a);
         c.launches += 1;

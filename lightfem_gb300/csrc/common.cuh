@@ -193,6 +193,20 @@ struct Context {
     unsigned int ic0_epoch = 0;
     i64 ic0_breakdowns = 0, ic0_levels = 0;
 
+    // Subdomain block-Jacobi (subdomain.cu): the split per (mesh, nodes per
+    // subdomain, split kind); the packed lower Cholesky factors per K version.
+    i64 sub_nodes = 64;  // the reference's defaults (subdomain_nodes 64, split rcb)
+    int sub_split = LFGPU_SPLIT_RCB;
+    unsigned long long sub_mesh_version = ~0ull, sub_k_version = ~0ull;
+    i64 sub_nodes_built = -1;
+    int sub_split_built = -1;
+    Buf<int> sub_dofs, sub_begin, sub_owner, sub_local;  // DOFs by subdomain; per DOF: subdomain, slot
+    Buf<long long> sub_fac_begin;
+    Buf<double> sub_factor;
+    i64 sub_count = 0, sub_degenerate = 0, sub_factor_size = 0;
+    int sub_max = 0;  // DOFs of the largest subdomain
+    double sub_capture = 0.0;
+
     lfgpu_timings timings{};
     i64 launches = 0;                 // kernels launched by this handle (graph nodes included)
     cudaEvent_t user_ev[8] = {};      // lfgpu_event_record slots

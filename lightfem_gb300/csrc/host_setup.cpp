@@ -7,6 +7,7 @@
 //                   src/sparse.cpp:15-74
 //   greedy_colors   element_colors, src/solver.cpp:100-133
 //   rcm_order       reverse_cuthill_mckee, src/reordering.cpp:11-62
+//   subdomain_split split_by_chunks / split_by_coordinates, src/precond.cpp:19-105
 //
 // A Q4 element couples both DOFs of each of its nodes, so rows 2i and 2i+1 share
 // one column list {2j, 2j+1 : j in S(i)} where S(i) is the set of nodes sharing an
@@ -190,6 +191,63 @@ void rcm_order(long long n_nodes, const long long* ids, long long n_elem, const 
         }
     }
     for (long long k = 0; k < n_nodes; ++k) order[k] = sorted[static_cast<size_t>(out[static_cast<size_t>(n_nodes - 1 - k)])];
+}
+
+long long subdomain_split(long long n_nodes, const double* xy, long long per, bool rcb, std::vector<uint32_t>& owner) {
+    const size_t nodes = static_cast<size_t>(std::max(0LL, n_nodes));
+    const size_t target = static_cast<size_t>(std::max(1LL, per));
+    owner.assign(nodes, 0);
+    if (nodes == 0) return 0;
+    if (!rcb) {
+        for (size_t k = 0; k < nodes; ++k) owner[k] = static_cast<uint32_t>(k / target);
+        return static_cast<long long>((nodes + target - 1) / target);
+    }
+    // Recursive bisection: the largest remaining range of the node permutation is
+    // cut at its median across the longer side of its bounding box until the
+    // wanted count is reached; ranges are numbered in the heap's storage order.
+    // The heap operations and the median selection are the standard library's,
+    // on size_t node indices, so ties between equal coordinates fall the same way
+    // as in the reference.
+    const size_t wanted = (nodes + target - 1) / target;
+    std::vector<size_t> perm(nodes);
+    std::iota(perm.begin(), perm.end(), size_t{0});
+    struct Span {
+        size_t first, last;  // [first, last) of perm
+    };
+    auto shorter = [](const Span& a, const Span& b) { return a.last - a.first < b.last - b.first; };
+    std::vector<Span> spans{Span{0, nodes}};
+    for (size_t have = 1; have < wanted; ++have) {
+        std::pop_heap(spans.begin(), spans.end(), shorter);
+        const Span cut = spans.back();
+        spans.pop_back();
+        if (cut.last - cut.first < 2) {  // only single nodes are left
+            spans.push_back(cut);
+            std::push_heap(spans.begin(), spans.end(), shorter);
+            break;
+        }
+        double lo_x = xy[2 * perm[cut.first]], hi_x = lo_x;
+        double lo_y = xy[2 * perm[cut.first] + 1], hi_y = lo_y;
+        for (size_t k = cut.first + 1; k < cut.last; ++k) {
+            const double px = xy[2 * perm[k]], py = xy[2 * perm[k] + 1];
+            lo_x = std::min(lo_x, px);
+            hi_x = std::max(hi_x, px);
+            lo_y = std::min(lo_y, py);
+            hi_y = std::max(hi_y, py);
+        }
+        const int axis = (hi_x - lo_x) >= (hi_y - lo_y) ? 0 : 1;
+        const size_t half = cut.first + (cut.last - cut.first) / 2;
+        std::nth_element(perm.begin() + static_cast<std::ptrdiff_t>(cut.first),
+                         perm.begin() + static_cast<std::ptrdiff_t>(half),
+                         perm.begin() + static_cast<std::ptrdiff_t>(cut.last),
+                         [&](size_t a, size_t b) { return xy[2 * a + axis] < xy[2 * b + axis]; });
+        spans.push_back(Span{cut.first, half});
+        std::push_heap(spans.begin(), spans.end(), shorter);
+        spans.push_back(Span{half, cut.last});
+        std::push_heap(spans.begin(), spans.end(), shorter);
+    }
+    for (size_t s = 0; s < spans.size(); ++s)
+        for (size_t k = spans[s].first; k < spans[s].last; ++k) owner[perm[k]] = static_cast<uint32_t>(s);
+    return static_cast<long long>(spans.size());
 }
 
 }  // namespace lfgpu

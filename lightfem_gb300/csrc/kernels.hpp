@@ -44,11 +44,16 @@ PcgResult run_pcg(Context& c, const SolveSetup& s, float* kernel_ms);
 
 // cg_graph.cu: the same solver as a device-driven CUDA graph of per-phase kernels
 PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms);
-// FP64 PCG with the IC(0) factor (triangular sweeps inside the graph); apply_ms is
-// the device time of one standalone application times the applications made.
-PcgResult run_pcg_ic0(Context& c, const SolveSetup& s, float* kernel_ms, double* apply_ms);
+// FP64 PCG with a preconditioner applied by its own kernels inside the graph: the
+// IC(0) triangular sweeps or the subdomain block solves.  apply_ms is the device
+// time of one standalone application times the applications made.
+PcgResult run_pcg_separate(Context& c, const SolveSetup& s, float* kernel_ms, double* apply_ms);
 // One FP64 application z = M^-1 r of the built preconditioner, on the stream.
 void launch_precond_apply(Context& c, int precond, const double* r, double* z);
+
+// subdomain.cu: subdomain block-Jacobi split (per mesh and setting) and factor
+// (per K version)
+void ensure_subdomains(Context& c);
 
 // ic0.cu: IC(0) factor of the constrained K on its own pattern (built per K version)
 enum Ic0Slot {

@@ -121,9 +121,18 @@ _MESSAGES = {
 }
 
 
+def gpu_preconditioner(settings) -> str:
+    """The library preconditioner for a reference setting: ``block`` with
+    ``subdomain_nodes 1`` is the 2x2 nodal form fused into the loop kernels; any
+    other size is the general subdomain block-Jacobi (``set_subdomains``)."""
+    if settings.preconditioner == "block" and int(settings.subdomain_nodes) != 1:
+        return "subdomain"
+    return settings.preconditioner
+
+
 def solve_options(settings) -> _native.SolveOptions:
     return _native.Context.options(settings.tolerance, settings.max_iterations, settings.storage,
-                                   settings.preconditioner, settings.precision, settings.refinement)
+                                   gpu_preconditioner(settings), settings.precision, settings.refinement)
 
 
 def set_mesh(ctx: _native.Context, model: Model) -> None:
@@ -182,6 +191,8 @@ class LinearElasticSolver:
         strategy = "atomic" if s.assembly == "atomic" or s.gpu_assembly == "atomic" else "coloring"
         ctx.assemble(strategy)
         ctx.apply_dirichlet()
+        if gpu_preconditioner(s) == "subdomain":
+            ctx.set_subdomains(s.subdomain_nodes, s.subdomain_split)
         try:
             u, rep = ctx.solve(solve_options(s))
         except _native.GpuError as err:

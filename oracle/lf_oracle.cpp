@@ -784,6 +784,25 @@ void lfo_bsr_convert(i64 n, const i64* ptr, const i64* col, const double* val, i
     std::copy(b.val.begin(), b.val.end(), bval);
 }
 
+// The node split of the block preconditioner (split: 0 chunk, 1 rcb; xy in node
+// index order); returns the subdomain count.
+i64 lfo_subdomain_split(i64 nodes, const double* xy, i64 nodes_per, int split, uint32_t* owner) {
+    size_t count = 0;
+    std::vector<uint32_t> o;
+    if (split == 0) {
+        o = chunk_split(static_cast<size_t>(nodes), static_cast<size_t>(nodes_per), &count);
+    } else {
+        std::vector<double> x(static_cast<size_t>(nodes)), y(static_cast<size_t>(nodes));
+        for (i64 k = 0; k < nodes; ++k) {
+            x[static_cast<size_t>(k)] = xy[2 * k];
+            y[static_cast<size_t>(k)] = xy[2 * k + 1];
+        }
+        o = rcb_split(x, y, static_cast<size_t>(nodes_per), &count);
+    }
+    std::copy(o.begin(), o.end(), owner);
+    return static_cast<i64>(count);
+}
+
 // One preconditioner application z = M^-1 r.  precond: 0 jacobi, 1 block, 2 ic0.
 // split: 0 chunk, 1 rcb (node coordinates in xy, node index order).
 int lfo_precond_apply(i64 n, const i64* ptr, const i64* col, const double* val, int precond, int split, i64 nodes_per,

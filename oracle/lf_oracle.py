@@ -53,6 +53,7 @@ def lib() -> ctypes.CDLL:
             "lfo_adjoint_grad": (i32, [vp, i64, vp, vp, vp, vp, i32, vp, vp, vp]),
             "lfo_postprocess": (i32, [vp, i64, i64, vp, vp, vp, i32, vp, vp, vp]),
             "lfo_rcm": (None, [i64, vp, i64, vp, vp]),
+            "lfo_subdomain_split": (i64, [i64, vp, i64, i32, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -135,6 +136,14 @@ def bsr(rp, col, val):
 PRECOND = {"jacobi": 0, "block": 1, "ic0": 2}
 SPLIT = {"chunk": 0, "rcb": 1}
 STORAGE = {"csr": 0, "bsr": 1}
+
+
+def subdomain_split(xy, nodes_per, split="rcb"):
+    """split_by_chunks / split_by_coordinates: (owner per node, subdomain count)."""
+    xy = _c(xy)
+    owner = np.empty(xy.shape[0], np.uint32)
+    count = lib().lfo_subdomain_split(xy.shape[0], _p(xy), int(nodes_per), SPLIT[split], _p(owner))
+    return owner, int(count)
 
 
 def precond_apply(rp, col, val, r, precond="jacobi", split="chunk", nodes_per=1, xy=None):

@@ -57,3 +57,19 @@ def test_create_without_gpu_fails_cleanly(native):
         pass
     with pytest.raises(native.GpuError):
         native.Context(0)
+
+
+def test_host_subdomains_match_oracle(native, oracle):
+    """The library's node split (split_by_chunks / split_by_coordinates,
+    src/precond.cpp:19-105) equals the oracle's, ties between equal coordinates
+    included, on structured, perturbed and reordered meshes."""
+    from lightfem_gb300 import mesh
+    meshes = [indexed(CASES[name]()) for name in ("grid6", "beam", "strain")]
+    meshes.append(indexed(mesh.workload(1)))
+    for model in meshes:
+        for per in (1, 2, 3, 7, 64, 100):
+            for split in ("rcb", "chunk"):
+                got, n_got = native.host_subdomains(model.xy, per, split)
+                want, n_want = oracle.subdomain_split(model.xy, per, split)
+                assert n_got == n_want
+                np.testing.assert_array_equal(got, want)

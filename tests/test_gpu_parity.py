@@ -17,7 +17,8 @@ from lightfem_gb300.solver import LinearElasticSolver, upload_model
 
 pytestmark = pytest.mark.gpu
 
-GPU_VARIANTS = ["csr_jacobi", "bsr_jacobi", "bsr_block1", "csr_block1", "csr_ic0", "bsr_ic0"]
+GPU_VARIANTS = ["csr_jacobi", "bsr_jacobi", "bsr_block1", "csr_block1", "csr_ic0", "bsr_ic0", "bsr_block_rcb2",
+                "bsr_block_chunk4"]
 
 
 def rel(a, b):
@@ -161,9 +162,10 @@ def test_pcg_fp64_matches_reference(native, golden_json, name, variant):
     if variant not in golden_json[name]:
         pytest.skip("variant not in the golden set")
     g = load_golden(name)
-    storage, precond, _, _ = VARIANTS[variant]
+    storage, precond, split, nodes = VARIANTS[variant]
     model = indexed(CASES[name]())
     model.settings.storage, model.settings.preconditioner = storage, precond
+    model.settings.subdomain_split, model.settings.subdomain_nodes = split, nodes
     res = LinearElasticSolver().solve(model)
     ref = golden_json[name][variant]
     assert abs(res.solver.iterations - ref["iterations"]) <= 2
@@ -295,6 +297,81 @@ def test_preconditioner_applications(native, oracle, name):
         np.testing.assert_array_equal(z, z_ref, err_msg=precond)
         assert rel(z, golden) <= 1e-10, precond
         assert ms > 0.0
+
+
+SUBDOMAIN_SPLITS = [("rcb", 2), ("chunk", 4), ("rcb", 7), ("rcb", 64), ("chunk", 64), ("rcb", 80), ("chunk", 200),
+                    ("rcb", 300)]
+
+
+@pytest.mark.parametrize("name", ["grid6", "beam", "strain"])
+def test_subdomain_preconditioner_applications(native, oracle, name):
+    """The general SubdomainBlockJacobi (any subdomain size, RCB or chunk split):
+    the device factor and block solves give the oracle's z bit for bit on the same
+    constrained K, and grid6's RCB-2 application matches the reference's golden z
+    within the assembly tolerance."""
+    model, ctx = prepared(native, name)
+    ctx.assemble("coloring")
+    ctx.apply_dirichlet()
+    Kc = ctx.download(native.K_CONSTRAINED)
+    fc = ctx.download(native.F_CONSTRAINED)
+    rp, col, _, _ = ctx.download_pattern()
+    for split, nodes in SUBDOMAIN_SPLITS:
+        ctx.set_subdomains(nodes, split)
+        z, ms = ctx.apply_preconditioner(fc, "subdomain")
+        z_ref, _ = oracle.precond_apply(rp, col, Kc, fc, "block", split, nodes, model.xy)
+        np.testing.assert_array_equal(z, z_ref, err_msg=f"{split} {nodes}")
+        assert ms > 0.0
+    if name == "grid6":
+        ctx.set_subdomains(2, "rcb")
+        z, _ = ctx.apply_preconditioner(fc, "subdomain")
+        assert rel(z, load_golden(name)["z_block"]) <= 1e-10
+
+
+def test_subdomain_over_the_limit_is_unsupported(native):
+    """A subdomain of more than LFGPU_SUBDOMAIN_MAX_DOFS DOFs is refused, and the
+    handle stays usable."""
+    model = indexed(mesh.cantilever(30, 20))
+    ctx = native.Context(0)
+    upload_model(ctx, model)
+    ctx.assemble("coloring")
+    ctx.apply_dirichlet()
+    fc = ctx.download(native.F_CONSTRAINED)
+    ctx.set_subdomains(native.SUBDOMAIN_MAX_DOFS // 2 + 1, "chunk")
+    with pytest.raises(native.GpuError) as err:
+        ctx.apply_preconditioner(fc, "subdomain")
+    assert err.value.code == native.ERR_UNSUPPORTED
+    ctx.set_subdomains(64, "rcb")
+    z, _ = ctx.apply_preconditioner(fc, "subdomain")
+    assert np.all(np.isfinite(z))
+
+
+@pytest.mark.parametrize("storage", ["csr", "bsr"])
+@pytest.mark.parametrize("split", ["rcb", "chunk"])
+def test_subdomain_solve_matches_oracle(native, oracle, storage, split):
+    """PCG with the reference's default block preconditioner (64-node subdomains)
+    on the perturbed two-material beam: iterations within 2 of the oracle's on the
+    same K, displacements within 1e-8, and the report's subdomain count, capture
+    ratio and degenerate count equal to the oracle's."""
+    model = indexed(CASES["beam"]())
+    model.settings.storage, model.settings.preconditioner = storage, "block"
+    model.settings.subdomain_split, model.settings.subdomain_nodes = split, 64
+    solver = LinearElasticSolver()
+    res = solver.solve(model)
+    ctx = solver.context
+    Kc = ctx.download(native.K_CONSTRAINED)
+    fc = ctx.download(native.F_CONSTRAINED)
+    rp, col, _, _ = ctx.download_pattern()
+    u_ref, rep = oracle.pcg(rp, col, Kc, fc, model.settings.tolerance, model.settings.max_iterations, storage,
+                            "block", split, 64, model.xy)
+    assert rep["converged"]
+    assert abs(res.solver.iterations - rep["iterations"]) <= 2
+    assert rel(res.displacement, u_ref) <= 1e-8
+    assert res.solver.subdomains == int(rep["stats"][0])
+    assert res.solver.capture_ratio == rep["stats"][1]
+    assert res.solver.preconditioner_setup_ms > 0.0 and res.solver.preconditioner_apply_ms > 0.0
+    model.settings.precision = "mixed"
+    with pytest.raises(RuntimeError, match="mixed precision supports"):
+        LinearElasticSolver().solve(model)
 
 
 @pytest.mark.parametrize("name", ["grid6", "beam", "strain"])
