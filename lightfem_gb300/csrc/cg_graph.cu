@@ -1010,15 +1010,16 @@ __global__ void __launch_bounds__(kThreads) ic0_dot(CgArgs a) {
 // unknown j is final every later row subtracts its term, so each row subtracts
 // its terms in the reference's order (ascending forward, descending backward),
 // each product and difference rounded on its own.  The result equals the
-// reference's bit for bit.
+// reference's bit for bit.  The kernel is bound by the FP64 pipe: a separate
+// multiply and subtract per factor entry and sweep.
 __global__ void __launch_bounds__(LFGPU_SUBDOMAIN_MAX_DOFS) subdomain_apply(CgArgs a) {
     __shared__ double v[LFGPU_SUBDOMAIN_MAX_DOFS];
     const int s = blockIdx.x, i = threadIdx.x;
     const int begin = a.sub_begin[s], D = a.sub_begin[s + 1] - begin;
-    const double* f = a.sub_factor + a.sub_fac[s];
+    const double* __restrict__ f = a.sub_factor + a.sub_fac[s];
     const bool mine = i < D;
     const int dof = mine ? a.sub_dofs[begin + i] : 0;
-    const double* row = f + static_cast<long long>(i) * (i + 1) / 2;  // this thread's factor row
+    const double* __restrict__ row = f + static_cast<long long>(i) * (i + 1) / 2;  // this thread's factor row
     double acc = mine ? a.r[dof] : 0.0;
     for (int j = 0; j < D; ++j) {
         if (i == j) v[j] = __dmul_rn(acc, row[j]);  // row[j] is the reciprocal pivot

@@ -110,6 +110,8 @@ CFG2_VARIANTS = {
     "block": ("storage=bsr", "preconditioner=block", "subdomain_split=chunk", "subdomain_nodes=1",
               "assembly=coloring"),
     "ic0": ("storage=csr", "preconditioner=ic0", "assembly=coloring"),
+    "block64": ("storage=bsr", "preconditioner=block", "subdomain_split=rcb", "subdomain_nodes=64",
+                "assembly=coloring"),
 }
 
 

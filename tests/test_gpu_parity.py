@@ -201,9 +201,7 @@ def test_cfg1_full_size(native, golden_json):
     g = load_golden("cfg1")
     ref = golden_json["cfg1"]
     for variant in ("csr_jacobi", "bsr_jacobi", "bsr_block1", "csr_ic0"):
-        storage, precond, _, _ = VARIANTS[variant]
-        model = indexed(mesh.workload(1))
-        model.settings.storage, model.settings.preconditioner = storage, precond
+        model = with_precond(indexed(mesh.workload(1)), *VARIANTS[variant])
         res = LinearElasticSolver(retain_matrix=False).solve(model)
         assert abs(res.solver.iterations - ref[variant]["iterations"]) <= 2, variant
         assert rel(res.displacement[::101], g[f"u_{variant}"]) <= 1e-8, variant
@@ -212,27 +210,39 @@ def test_cfg1_full_size(native, golden_json):
         assert res.solver.true_residual <= 1.01e-8 * ref[variant]["initial_residual"]
 
 
-CFG2 = {"jacobi": ("csr", "jacobi"), "bsr_jacobi": ("bsr", "jacobi"), "block": ("bsr", "block")}
+def with_precond(model, storage, precond, split="chunk", nodes=1):
+    """Storage and preconditioner settings; ``block`` defaults to 2x2 nodal blocks
+    (the reference's block with subdomain_nodes 1)."""
+    s = model.settings
+    s.storage, s.preconditioner, s.subdomain_split, s.subdomain_nodes = storage, precond, split, nodes
+    return model
+
+
+# storage, preconditioner, subdomain split, nodes per subdomain
+CFG2 = {"jacobi": ("csr", "jacobi", "chunk", 1), "bsr_jacobi": ("bsr", "jacobi", "chunk", 1),
+        "block": ("bsr", "block", "chunk", 1), "block64": ("bsr", "block", "rcb", 64)}
 
 
 @pytest.mark.parametrize("variant", list(CFG2))
 def test_cfg2_full_size(native, golden_json, variant):
     """The 1000x1000 workload (2,004,002 DOFs, RCM) against the reference's own runs:
     FP64 PCG iteration count within 2, displacements within 1e-8; the mixed solve
-    reaches the same true-residual target."""
+    reaches the same true-residual target.  block64 is the reference's default
+    block preconditioner (64-node RCB subdomains, FP64 only)."""
     ref = golden_json["cfg2"][variant]
     g = load_golden("cfg2")
-    storage, precond = CFG2[variant]
-    model = indexed(mesh.workload(2))
-    model.settings.storage, model.settings.preconditioner = storage, precond
+    model = with_precond(indexed(mesh.workload(2)), *CFG2[variant])
     res = LinearElasticSolver(retain_matrix=False, postprocess=False).solve(model)
     assert abs(res.solver.iterations - ref["iterations"]) <= 2
     u = by_id_order(model, res.displacement)
     assert rel(u[::2003], g[f"u_{variant}"]) <= 1e-8
     assert np.linalg.norm(u) == pytest.approx(ref["u_norm"], rel=1e-8)
     assert abs(res.reaction[1::2].sum() - ref["R_y_sum"]) <= 1e-6
-    mixed = indexed(mesh.workload(2))
-    mixed.settings.storage, mixed.settings.preconditioner, mixed.settings.precision = storage, precond, "mixed"
+    if variant == "block64":
+        assert res.solver.subdomains == 15657 and res.solver.capture_ratio == ref["capture_ratio"]
+        return
+    mixed = with_precond(indexed(mesh.workload(2)), *CFG2[variant])
+    mixed.settings.precision = "mixed"
     rm = LinearElasticSolver(retain_matrix=False, postprocess=False).solve(mixed)
     assert rm.solver.true_residual <= 1.001e-8 * rm.solver.initial_residual
     assert rel(by_id_order(mixed, rm.displacement), u) <= 1e-6
@@ -244,8 +254,7 @@ def test_cfg3_full_size_mixed_vs_fp64(native):
     the 1e-8 target and agree; the reactions balance the applied loads."""
     sols = {}
     for precision in ("fp64", "mixed"):
-        model = indexed(mesh.workload(3))
-        model.settings.storage, model.settings.preconditioner = "bsr", "block"
+        model = with_precond(indexed(mesh.workload(3)), "bsr", "block")
         model.settings.precision = precision
         res = LinearElasticSolver(retain_matrix=False, postprocess=False).solve(model)
         target = 1e-8 * res.solver.initial_residual
@@ -263,8 +272,7 @@ def test_cfg3_full_size_mixed_vs_fp64(native):
 @pytest.mark.parametrize("precond", ["jacobi", "block"])
 @pytest.mark.parametrize("refinement", ["reliable", "restart"])
 def test_mixed_precision_reaches_fp64_target(native, storage, precond, refinement):
-    model = indexed(mesh.workload(1, scale=4))
-    model.settings.storage, model.settings.preconditioner = storage, precond
+    model = with_precond(indexed(mesh.workload(1, scale=4)), storage, precond)
     fp64 = LinearElasticSolver().solve(model.copy())
     model.settings.precision, model.settings.refinement = "mixed", refinement
     res = LinearElasticSolver().solve(model)
@@ -396,7 +404,7 @@ def test_postprocess_fields(native, oracle, name):
 def test_ic0_rejects_mixed_precision(native):
     model = indexed(CASES["grid6"]())
     model.settings.preconditioner, model.settings.precision = "ic0", "mixed"
-    with pytest.raises(RuntimeError, match="mixed precision supports the jacobi and block"):
+    with pytest.raises(RuntimeError, match="mixed precision supports the jacobi and 2x2 block"):
         LinearElasticSolver().solve(model)
 
 
