@@ -372,8 +372,11 @@ def run_ours(args) -> int:
     if args.profile_iters:
         # Profiling run (not a benchmark): one step with the PCG capped at
         # --profile-iters iterations, the same loop with its kernels launched on the
-        # stream, then three standalone products of each kind.  IC(0) runs in FP64.
-        precision = "fp64" if args.precond == "ic0" else "mixed"
+        # stream, then three standalone products of each kind.  IC(0) and the
+        # subdomain blocks run in FP64.
+        precision = "fp64" if args.precond in ("ic0", "subdomain") else "mixed"
+        if args.precond == "subdomain":
+            ctx.set_subdomains(args.subdomain_nodes, args.subdomain_split)
         capped = ctx.options(tol, args.profile_iters, args.storage, args.precond, precision, "reliable")
         ms, rep = step(capped)
         unrolled = ctx.options(tol, 10 ** 6, args.storage, args.precond, precision, "reliable",
@@ -554,8 +557,10 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--storage", choices=("csr", "bsr"), default="bsr")
-    ap.add_argument("--precond", choices=("jacobi", "block", "ic0"), default="jacobi",
-                    help="ic0 only with --profile-iters (FP64 profiling run)")
+    ap.add_argument("--precond", choices=("jacobi", "block", "ic0", "subdomain"), default="jacobi",
+                    help="block: 2x2 nodal blocks; ic0 and subdomain only with --profile-iters (FP64 profiling run)")
+    ap.add_argument("--subdomain-nodes", type=int, default=64, help="nodes per subdomain for --precond subdomain")
+    ap.add_argument("--subdomain-split", choices=("rcb", "chunk"), default="rcb")
     ap.add_argument("--scale", type=int, default=1, help="divide the mesh size (testing only)")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -568,8 +573,8 @@ def main() -> int:
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling run for ncu: one step capped at this many PCG iterations (not a benchmark)")
     args = ap.parse_args()
-    if args.precond == "ic0" and not args.profile_iters:
-        ap.error("--precond ic0 is a profiling option (use it with --profile-iters)")
+    if args.precond in ("ic0", "subdomain") and not args.profile_iters:
+        ap.error(f"--precond {args.precond} is a profiling option (use it with --profile-iters)")
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")
     return run_reference(args) if args.impl == "reference" else run_ours(args)

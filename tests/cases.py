@@ -201,6 +201,7 @@ VARIANTS = {
     "csr_block1": ("csr", "block", "chunk", 1),
     "bsr_block_rcb2": ("bsr", "block", "rcb", 2),
     "bsr_block_chunk4": ("bsr", "block", "chunk", 4),
+    "bsr_block64": ("bsr", "block", "rcb", 64),
 }
 
 

@@ -100,6 +100,7 @@ VARIANTS = {
     "csr_block1": ("storage=csr", "preconditioner=block", "subdomain_split=chunk", "subdomain_nodes=1"),
     "bsr_block_rcb2": ("storage=bsr", "preconditioner=block", "subdomain_split=rcb", "subdomain_nodes=2"),
     "bsr_block_chunk4": ("storage=bsr", "preconditioner=block", "subdomain_split=chunk", "subdomain_nodes=4"),
+    "bsr_block64": ("storage=bsr", "preconditioner=block", "subdomain_split=rcb", "subdomain_nodes=64"),
 }
 
 
@@ -208,7 +209,7 @@ def main() -> None:
         tolerance=1e-10, max_iterations=20000, assembly="coloring"))
     arrays, report = run(model, "pattern=1", "ke=4", "precond=1", "subdomain_split=chunk", "subdomain_nodes=1")
     golden["beam"] = {"pattern": report}
-    for vname in ("csr_jacobi", "bsr_jacobi", "csr_ic0", "bsr_block1"):
+    for vname in ("csr_jacobi", "bsr_jacobi", "csr_ic0", "bsr_block1", "bsr_block64"):
         va, vr = run(model, "solve=1", *VARIANTS[vname])
         arrays[f"u_{vname}"] = va["u"]
         arrays[f"R_{vname}"] = va["R"]
@@ -224,7 +225,7 @@ def main() -> None:
                                                     reordering="rcm"))
     arrays, report = run(model, "pattern=1", "ke=2", "precond=1", "subdomain_split=chunk", "subdomain_nodes=1")
     golden["strain"] = {"pattern": report}
-    for vname in ("csr_jacobi", "csr_ic0", "bsr_block1"):
+    for vname in ("csr_jacobi", "csr_ic0", "bsr_block1", "bsr_block64"):
         va, vr = run(model, "solve=1", *VARIANTS[vname])
         arrays[f"u_{vname}"] = va["u"]
         arrays[f"R_{vname}"] = va["R"]
@@ -258,7 +259,7 @@ def main() -> None:
             "map_sum": np.array([arrays["map"].sum()]), "K_sample": arrays["K"][::997],
             "Kc_sample": arrays["Kc"][::997], "fc": arrays["fc"], "colors": arrays["colors"]}
     golden["cfg1"] = {"pattern": report, "nnz": int(arrays["col"].shape[0])}
-    for vname in ("csr_jacobi", "bsr_jacobi", "csr_ic0", "bsr_block1"):
+    for vname in ("csr_jacobi", "bsr_jacobi", "csr_ic0", "bsr_block1", "bsr_block64"):
         va, vr = run(model, "solve=1", *VARIANTS[vname])
         keep[f"u_{vname}"] = va["u"][::101]
         keep[f"R_{vname}"] = va["R"][::101]

@@ -18,7 +18,7 @@ from lightfem_gb300.solver import LinearElasticSolver, upload_model
 pytestmark = pytest.mark.gpu
 
 GPU_VARIANTS = ["csr_jacobi", "bsr_jacobi", "bsr_block1", "csr_block1", "csr_ic0", "bsr_ic0", "bsr_block_rcb2",
-                "bsr_block_chunk4"]
+                "bsr_block_chunk4", "bsr_block64"]
 
 
 def rel(a, b):
@@ -200,7 +200,7 @@ def test_cfg1_full_size(native, golden_json):
     """The 200x200 workload against the reference's iteration counts and fields."""
     g = load_golden("cfg1")
     ref = golden_json["cfg1"]
-    for variant in ("csr_jacobi", "bsr_jacobi", "bsr_block1", "csr_ic0"):
+    for variant in ("csr_jacobi", "bsr_jacobi", "bsr_block1", "csr_ic0", "bsr_block64"):
         model = with_precond(indexed(mesh.workload(1)), *VARIANTS[variant])
         res = LinearElasticSolver(retain_matrix=False).solve(model)
         assert abs(res.solver.iterations - ref[variant]["iterations"]) <= 2, variant

@@ -140,7 +140,7 @@ def test_cfg1_known_answers(oracle, golden_json):
     np.testing.assert_array_equal(out["Kc"][::997], g["Kc_sample"])
     np.testing.assert_array_equal(out["fc"], g["fc"])
     np.testing.assert_array_equal(out["colors"], g["colors"])
-    for v in ("csr_jacobi", "bsr_jacobi", "bsr_block1"):
+    for v in ("csr_jacobi", "bsr_jacobi", "bsr_block1", "bsr_block64"):
         storage, precond, split, per = VARIANTS[v]
         u, rep = oracle.pcg(out["rowptr"], out["col"], out["Kc"], out["fc"], 1e-8, 200000, storage, precond,
                             split, per, model.xy)
