@@ -115,7 +115,8 @@ typedef struct lfgpu_report {
     double solve_ms;                 /* device time of the solve (CUDA events) */
     double matvec_ms;                /* device time of one standalone SpMV x matvec_calls */
     int64_t matvec_calls;
-    int64_t matrix_bytes_per_matvec; /* bytes of the matrix one product streams */
+    int64_t matrix_bytes_per_matvec; /* bytes of the matrix one product streams (int32 columns; mixed BSR:
+                                        16-bit column offsets when they fit) */
     double storage_convert_ms;
     double preconditioner_setup_ms;
     double preconditioner_apply_ms;  /* IC0 only: device time of the triangular sweeps */

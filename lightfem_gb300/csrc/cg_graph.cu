@@ -50,6 +50,7 @@ struct CgArgs {
     const float* K32;
     const int* brow;
     const int* bcol;
+    const short* bcol16;           // FP32 BSR: columns as offsets from the block row, or nullptr
     const double2* bval64;
     const float4* bval32;
     const float* dhi;
@@ -288,12 +289,14 @@ __device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& ou
         float s0 = 0.f, s1 = 0.f;
         if (act) {
             const int b = __ldg(a.brow + node), e = __ldg(a.brow + node + 1);
+            // Columns as 16-bit offsets from the block row when they fit (half the bytes).
+            auto col = [&](int k) { return a.bcol16 ? node + ld_stream(a.bcol16 + k) : ld_stream(a.bcol + k); };
             for (int k = b + sub; k < e; k += 12) {
                 const bool t1 = k + 4 < e, t2 = k + 8 < e;
                 const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-                const int c0 = ld_stream(a.bcol + k);
-                const int c1 = t1 ? ld_stream(a.bcol + k + 4) : c0;
-                const int c2 = t2 ? ld_stream(a.bcol + k + 8) : c0;
+                const int c0 = col(k);
+                const int c1 = t1 ? col(k + 4) : c0;
+                const int c2 = t2 ? col(k + 8) : c0;
                 const float4 v0 = ld_stream(a.bval32 + k);
                 const float4 v1 = t1 ? ld_stream(a.bval32 + k + 4) : zero;
                 const float4 v2 = t2 ? ld_stream(a.bval32 + k + 8) : zero;
@@ -1311,6 +1314,7 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         if (s.storage == LFGPU_STORAGE_BSR) {
             ensure_bsr32(c);
             a.bval32 = reinterpret_cast<const float4*>(c.bval32.p);
+            a.bcol16 = c.bcol16_ok ? c.bcol16.p : nullptr;
         } else {
             ensure_csr32(c);
             a.K32 = c.K32;

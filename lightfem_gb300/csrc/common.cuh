@@ -139,6 +139,8 @@ struct Context {
     Buf<int> brow, bcol;
     Buf<double> bval64;
     Buf<float> bval32;
+    Buf<short> bcol16;      // FP32 BSR columns as offsets from the block row, when all fit in 16 bits
+    bool bcol16_ok = false;
     Buf<float> K32;
     i64 nblocks = 0;
     unsigned long long bsr_version = ~0ull, k32_version = ~0ull, b32_version = ~0ull;
@@ -233,6 +235,7 @@ __device__ __forceinline__ T warp_sum(T v) {
 __device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
 __device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int* p) { return __ldcs(p); }
+__device__ __forceinline__ short ld_stream(const short* p) { return __ldcs(p); }
 __device__ __forceinline__ double2 ld_stream(const double2* p) { return __ldcs(p); }
 __device__ __forceinline__ float4 ld_stream(const float4* p) { return __ldcs(p); }
 __device__ __forceinline__ int2 ld_stream(const int2* p) { return __ldcs(p); }

@@ -503,6 +503,22 @@ void launch_to_float(Context& c, const double* in, float* out, i64 count) {
     LF_CUDA(cudaGetLastError());
 }
 
+// Block columns as 16-bit offsets from the block row (the FP32 product's column
+// stream at half the bytes); *wide is set when an offset does not fit.
+__global__ void bsr_offsets_kernel(int nb, const int* __restrict__ brow, const int* __restrict__ bcol,
+                                   short* __restrict__ off, int* __restrict__ wide) {
+    const int node = blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nb) return;
+    for (int k = brow[node]; k < brow[node + 1]; ++k) {
+        const int d = bcol[k] - node;
+        if (d < -32768 || d > 32767) {
+            atomicOr(wide, 1);
+            return;
+        }
+        off[k] = static_cast<short>(d);
+    }
+}
+
 void ensure_bsr32(Context& c) {
     ensure_bsr(c);
     if (c.b32_version == c.k_version) return;
@@ -517,7 +533,17 @@ void ensure_bsr32(Context& c) {
                                                                                c.col, c.K, nullptr, c.diag_hi,
                                                                                c.diag_lo);
     c.launches += 1;
+    c.bcol16.ensure(static_cast<size_t>(c.nblocks));
+    c.scratch64.ensure(64);
+    int* wide = reinterpret_cast<int*>(c.scratch64.p + 40);
+    LF_CUDA(cudaMemsetAsync(wide, 0, sizeof(int), c.stream));
+    bsr_offsets_kernel<<<grid_for(nb, kThreads), kThreads, 0, c.stream>>>(nb, c.brow, c.bcol, c.bcol16, wide);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
+    int h = 0;
+    LF_CUDA(cudaMemcpyAsync(&h, wide, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    LF_CUDA(cudaStreamSynchronize(c.stream));
+    c.bcol16_ok = h == 0;
     c.b32_version = c.k_version;
 }
 
