@@ -70,7 +70,7 @@ enum { LFGPU_ASSEMBLY_COLORING = 0, LFGPU_ASSEMBLY_ATOMIC = 1 };
 enum { LFGPU_STORAGE_CSR = 0, LFGPU_STORAGE_BSR = 1 };
 /* BLOCK2: the 2x2 nodal case (subdomain_nodes 1) fused into the loop kernels.
  * SUBDOMAIN: SubdomainBlockJacobi with the handle's lfgpu_set_subdomains split
- * (the reference's `preconditioner block` with any subdomain_nodes); FP64 only. */
+ * (the reference's `preconditioner block` with any subdomain_nodes). */
 enum { LFGPU_PRECOND_JACOBI = 0, LFGPU_PRECOND_BLOCK2 = 1, LFGPU_PRECOND_IC0 = 2, LFGPU_PRECOND_SUBDOMAIN = 3 };
 enum { LFGPU_SPLIT_RCB = 0, LFGPU_SPLIT_CHUNK = 1 };
 enum { LFGPU_PRECISION_FP64 = 0, LFGPU_PRECISION_MIXED = 1 };

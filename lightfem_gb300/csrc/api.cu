@@ -539,7 +539,9 @@ lfgpu::PcgResult finish_in_fp64(lfgpu_t h, const lfgpu_solve_options* o, const l
     f.x0 = x0.p;
     f.max_iterations = std::max<i64>(1, s.max_iterations - done_iterations);
     float ms2 = 0.f;
-    const PcgResult r2 = o->persistent ? run_pcg(*h, f, &ms2) : run_cg_graph(*h, f, &ms2);
+    const PcgResult r2 = f.precond == LFGPU_PRECOND_SUBDOMAIN ? run_pcg_separate(*h, f, &ms2, nullptr)
+                         : o->persistent                       ? run_pcg(*h, f, &ms2)
+                                                               : run_cg_graph(*h, f, &ms2);
     *ms += ms2;
     return r2;
 }
@@ -559,8 +561,8 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
                    LFGPU_ERR_ARGUMENT, "preconditioner must be jacobi, block, ic0 or subdomain");
         LF_REQUIRE(o->precision == LFGPU_PRECISION_FP64 || o->precision == LFGPU_PRECISION_MIXED, LFGPU_ERR_ARGUMENT,
                    "precision must be fp64 or mixed");
-        LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner >= LFGPU_PRECOND_IC0),
-                   LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi and 2x2 block preconditioners");
+        LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner == LFGPU_PRECOND_IC0),
+                   LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi, block and subdomain preconditioners");
         lfgpu_report r{};
         r.status = LFGPU_OK;
         const double fnorm = device_norm2(*h, h->f, h->n);
@@ -600,8 +602,12 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
             LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
             r.preconditioner_setup_ms = elapsed_ms(*h);
             if (o->storage == LFGPU_STORAGE_BSR) ensure_bsr(*h);
-            res = run_pcg_separate(*h, s, &ms, &apply_ms);
-            r.preconditioner_apply_ms = apply_ms;
+            if (s.mixed) {
+                res = run_cg_graph(*h, s, &ms);
+            } else {
+                res = run_pcg_separate(*h, s, &ms, &apply_ms);
+                r.preconditioner_apply_ms = apply_ms;
+            }
             r.subdomains = h->sub_count;
             r.capture_ratio = h->sub_capture;
             r.degenerate_subdomains = h->sub_degenerate;
@@ -864,8 +870,8 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
             LF_REQUIRE(o != nullptr, LFGPU_ERR_ARGUMENT, "the adjoint solve needs solve options");
             LF_REQUIRE(o->preconditioner >= LFGPU_PRECOND_JACOBI && o->preconditioner <= LFGPU_PRECOND_SUBDOMAIN,
                        LFGPU_ERR_ARGUMENT, "preconditioner must be jacobi, block, ic0 or subdomain");
-            LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner >= LFGPU_PRECOND_IC0),
-                       LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi and 2x2 block preconditioners");
+            LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner == LFGPU_PRECOND_IC0),
+                       LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi, block and subdomain preconditioners");
             // Solve K lambda = dJ/du with dJ/du zeroed on the constrained DOFs: reuse the
             // solve machinery on the adjoint right-hand side.
             std::vector<double> rhs(dj_du, dj_du + n);
@@ -899,7 +905,7 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
             if (o->preconditioner == LFGPU_PRECOND_IC0 || o->preconditioner == LFGPU_PRECOND_SUBDOMAIN) {
                 if (o->preconditioner == LFGPU_PRECOND_IC0) ensure_ic0(*h);
                 else ensure_subdomains(*h);
-                res = run_pcg_separate(*h, s, &ms, &apply_ms);
+                res = s.mixed ? run_cg_graph(*h, s, &ms) : run_pcg_separate(*h, s, &ms, &apply_ms);
             } else {
                 ensure_preconditioners(*h, o->preconditioner);
                 res = o->persistent ? run_pcg(*h, s, &ms) : run_cg_graph(*h, s, &ms);

@@ -84,6 +84,7 @@ struct CgArgs {
     const int* sub_begin;
     const long long* sub_fac;      // packed lower factor offset of each subdomain
     const double* sub_factor;
+    const float* sub_factor32;     // FP32 copy for the mixed loop
     int blocks;
     CgState* st;
     DeviceStatus* status;
@@ -546,15 +547,19 @@ __device__ __forceinline__ void pair_axpy(float& hi, float& lo, float ah, float 
     lo = __fsub_rn(l, __fsub_rn(hi, s));
 }
 
+// The subdomain preconditioner is applied by its own kernel (mx_sub_apply) after
+// mx_init and after every mx_update: those two leave z and r.z to it.
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
+    constexpr bool kSub = PRECOND == LFGPU_PRECOND_SUBDOMAIN;
     double v[2] = {0.0, 0.0};
     const double2* f2 = reinterpret_cast<const double2*>(a.f);
     float4* zp = reinterpret_cast<float4*>(a.zp0);
     GRID_NODES(i) {
         const double2 fv = f2[i];
         const float2 rv = make_float2(static_cast<float>(fv.x), static_cast<float>(fv.y));
-        const float2 zv = precond32<PRECOND>(a, i, rv);
+        float2 zv = make_float2(0.f, 0.f);
+        if constexpr (!kSub) zv = precond32<PRECOND>(a, i, rv);
         reinterpret_cast<double2*>(a.x)[i] = make_double2(0.0, 0.0);
         reinterpret_cast<float2*>(a.xhi)[i] = make_float2(0.f, 0.f);
         reinterpret_cast<float2*>(a.xlo)[i] = make_float2(0.f, 0.f);
@@ -575,7 +580,7 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
         if (s->r0 <= a.target) {
             s->converged = 1;
             s->done = 1;
-        } else if (!(t[1] > 0.0) || !isfinite(t[1])) {
+        } else if (!kSub && (!(t[1] > 0.0) || !isfinite(t[1]))) {
             s->status = LFGPU_ERR_RHO_INITIAL;
             s->done = 1;
         }
@@ -641,6 +646,7 @@ __global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
 // x += alpha p (into the FP32 pair), r -= alpha q, z = M^-1 r; r.r and r.z.
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
+    constexpr bool kSub = PRECOND == LFGPU_PRECOND_SUBDOMAIN;
     if (a.st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_branch(a, false);
         return;
@@ -661,13 +667,14 @@ __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
         pair_axpy(hv.y, lv.y, alpha, alpha_lo, pv.y);
         rv.x -= alpha * qv.x;
         rv.y -= alpha * qv.y;
-        const float2 zv = precond32<PRECOND>(a, i, rv);
+        float2 zv = make_float2(0.f, 0.f);
+        if constexpr (!kSub) zv = precond32<PRECOND>(a, i, rv);
         hi2[i] = hv;
         lo2[i] = lv;
         r2[i] = rv;
         zp_next[i] = make_float4(zv.x, pv.x, zv.y, pv.y);
         rr.add(rv.x * rv.x + rv.y * rv.y);
-        rz.add(rv.x * zv.x + rv.y * zv.y);
+        if constexpr (!kSub) rz.add(rv.x * zv.x + rv.y * zv.y);
     }
     FloatPair v[2] = {rr, rz};
     reduce_last<2>(a, 2, v, [&](const double* t) {
@@ -678,7 +685,7 @@ __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
         s->rmax = fmax(s->rmax, rn);
         const bool refine = rn <= a.reduction * s->rmax || rn <= a.target || s->it >= a.maxit;
         s->refine = refine;
-        if (!refine) {
+        if (!refine && !kSub) {
             if (!(t[1] > 0.0) || !isfinite(t[1])) {
                 s->status = LFGPU_ERR_RHO;
                 s->done = 1;
@@ -1039,6 +1046,104 @@ __global__ void __launch_bounds__(LFGPU_SUBDOMAIN_MAX_DOFS) subdomain_apply(CgAr
     if (mine) a.z[dof] = x;
 }
 
+// The mixed loop's application of the subdomain preconditioner: the same block
+// solves in FP32 (an FP32 copy of the factor, fused multiply-adds) on r32, z
+// into the (z, p) copy the next product reads, and r.z.  Its reduction sets rho
+// and beta: after mx_init the first rho (r0.z0 > 0 or "positive initial
+// preconditioned residual"), in the loop beta = r.z / rho, or 0 after a residual
+// replacement in restart mode.
+//
+// In FP32 a step is a few cycles, so a CTA barrier per unknown would dominate.
+// The solves run in tiles of 32 rows instead.  The warp that owns the diagonal
+// tile resolves its 32 unknowns one by one with shuffles.  After one barrier,
+// every later row subtracts the tile's 32 terms.  Each row still subtracts its
+// terms in ascending order forward and descending order backward.
+__global__ void __launch_bounds__(LFGPU_SUBDOMAIN_MAX_DOFS) mx_sub_apply(CgArgs a) {
+    if (a.st->done) return;
+    __shared__ float v[LFGPU_SUBDOMAIN_MAX_DOFS];
+    const int s = blockIdx.x, i = threadIdx.x, lane = i & 31, wid = i >> 5;
+    const int begin = a.sub_begin[s], D = a.sub_begin[s + 1] - begin;
+    const float* __restrict__ f = a.sub_factor32 + a.sub_fac[s];
+    const bool mine = i < D;
+    const int dof = mine ? a.sub_dofs[begin + i] : 0;
+    const float* __restrict__ row = f + static_cast<long long>(i) * (i + 1) / 2;  // row i of L
+    const float r = mine ? a.r32[dof] : 0.f;
+    const int tiles = (D + 31) / 32;
+    float acc = r;
+    for (int t = 0; t < tiles; ++t) {  // forward: L y = r
+        const int t0 = 32 * t, cnt = min(32, D - t0);
+        if (wid == t) {
+            float dg[32];  // this row's entries in the tile (the reciprocal pivot at u == lane), loaded first
+#pragma unroll
+            for (int u = 0; u < 32; ++u) dg[u] = (mine && u <= lane && u < cnt) ? row[t0 + u] : 0.f;
+#pragma unroll
+            for (int u = 0; u < 32; ++u) {
+                if (u < cnt) {
+                    float vj = lane == u ? acc * dg[u] : 0.f;
+                    vj = __shfl_sync(0xffffffffu, vj, u);
+                    if (mine && lane > u) acc = fmaf(-dg[u], vj, acc);
+                    if (lane == u) v[t0 + u] = vj;
+                }
+            }
+        }
+        __syncthreads();
+        if (mine && wid > t) {
+#pragma unroll 8
+            for (int u = 0; u < cnt; ++u) acc = fmaf(-row[t0 + u], v[t0 + u], acc);
+        }
+    }
+    acc = mine ? v[i] : 0.f;  // this thread's own y
+    float x = 0.f;
+    for (int t = tiles - 1; t >= 0; --t) {  // backward: L^T z = y
+        const int t0 = 32 * t, cnt = min(32, D - t0);
+        if (wid == t) {
+            float dg[32];  // L(k, i) for the tile's rows k >= i (the reciprocal pivot at k == i), loaded first
+#pragma unroll
+            for (int u = 0; u < 32; ++u) {
+                const int k = t0 + u;
+                dg[u] = (u >= lane && u < cnt) ? f[static_cast<long long>(k) * (k + 1) / 2 + i] : 0.f;
+            }
+#pragma unroll
+            for (int u = 31; u >= 0; --u) {
+                if (u < cnt) {
+                    float xk = lane == u ? acc * dg[u] : 0.f;
+                    xk = __shfl_sync(0xffffffffu, xk, u);
+                    if (lane < u) acc = fmaf(-dg[u], xk, acc);
+                    if (lane == u) v[t0 + u] = x = xk;
+                }
+            }
+        }
+        __syncthreads();
+        if (mine && wid < t) {
+#pragma unroll 8
+            for (int u = cnt - 1; u >= 0; --u) {
+                const int k = t0 + u;
+                acc = fmaf(-f[static_cast<long long>(k) * (k + 1) / 2 + i], v[k], acc);
+            }
+        }
+    }
+    FloatPair rz;
+    if (mine) {
+        // z of DOF 2m sits in .x of node m's (z, p) float4, z of DOF 2m + 1 in .z.
+        reinterpret_cast<float*>(zp_buffer(a, a.st->it))[4 * (dof >> 1) + 2 * (dof & 1)] = x;
+        rz.add(r * x);
+    }
+    FloatPair vv[1] = {rz};
+    reduce_last<1>(a, 2, vv, [&](const double* t) {
+        CgState* st = a.st;
+        const bool first = st->it == 0;
+        if (!(t[0] > 0.0) || !isfinite(t[0])) {
+            st->status = first ? LFGPU_ERR_RHO_INITIAL : LFGPU_ERR_RHO;
+            st->done = 1;
+        } else {
+            st->beta = (first || (a.restart && st->refine)) ? 0.0 : t[0] / st->rho;
+            st->beta32 = static_cast<float>(st->beta);
+            st->rho = t[0];
+        }
+        set_loop(a, !st->done);
+    });
+}
+
 // One FP64 application of the Jacobi or 2x2 nodal preconditioner.
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) precond_apply_kernel(CgArgs a) {
@@ -1098,10 +1203,19 @@ void build_fp64(cudaGraph_t g, CgArgs* a, int blocks) {
 
 constexpr int kBodyIterations = 8;
 
+// The subdomain preconditioner (sub_grid CTAs of sub_threads) adds its own kernel
+// after mx_init and after each iteration's IF node; the branch then holds only
+// the flush and the FP64 residual, as the kernel after it re-preconditions.
 template <int STORAGE, int PRECOND>
-void build_mixed(cudaGraph_t g, CgArgs* a, int blocks) {
+void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub_threads = 0) {
+    constexpr bool kSub = PRECOND == LFGPU_PRECOND_SUBDOMAIN;
     cudaGraphNode_t n_init;
     add_kernel(g, &n_init, nullptr, 0, mx_init<PRECOND>, blocks, a);
+    if constexpr (kSub) {
+        cudaGraphNode_t n_apply;
+        add_kernel(g, &n_apply, &n_init, 1, mx_sub_apply, sub_grid, a, 0, sub_threads);
+        n_init = n_apply;
+    }
     cudaGraph_t body;
     const cudaGraphNode_t n_loop = add_conditional(g, &n_init, 1, a->loop, cudaGraphCondTypeWhile, &body);
     cudaGraphNode_t n_flush;
@@ -1123,7 +1237,12 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks) {
         prev = add_conditional(body, &k2, 1, ah->branch, cudaGraphCondTypeIf, &branch);
         add_kernel(branch, &k3, nullptr, 0, mx_flush<false>, blocks, ah);
         add_kernel(branch, &k4, &k3, 1, mx_residual<STORAGE>, blocks, ah);
-        add_kernel(branch, &k5, &k4, 1, mx_reprecondition<PRECOND>, blocks, ah);
+        if constexpr (kSub) {
+            add_kernel(body, &k5, &prev, 1, mx_sub_apply, sub_grid, ah, 0, sub_threads);
+            prev = k5;
+        } else {
+            add_kernel(branch, &k5, &k4, 1, mx_reprecondition<PRECOND>, blocks, ah);
+        }
     }
 }
 
@@ -1162,25 +1281,34 @@ struct EventTrail {
 // loop passes (the branch kernels run every pass and return unless a replacement
 // is due).  Profilers see these launches; they do not descend into graph nodes.
 // Phase slots: 0 product, 1 update, 2 FP64 p update or mixed residual
-// replacement, 3 mixed re-preconditioning.
+// replacement, 3 mixed re-preconditioning (subdomain: the block solves).
 template <int STORAGE, int PRECOND>
-void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int iters, EventTrail& trail) {
+void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int iters, EventTrail& trail,
+                     int sub_grid = 0, int sub_threads = 0) {
+    constexpr bool kSub = PRECOND == LFGPU_PRECOND_SUBDOMAIN;
     auto chain = [&](auto kernel, int phase) {
         kernel<<<blocks, kThreads, 0, stream>>>(*a);
         LF_CUDA(cudaGetLastError());
         trail.mark(phase);
     };
+    auto sub_apply = [&](int phase) {
+        mx_sub_apply<<<sub_grid, sub_threads, 0, stream>>>(*a);
+        LF_CUDA(cudaGetLastError());
+        trail.mark(phase);
+    };
     if (!mixed && a->x0) chain(cg64_residual<STORAGE>, -1);
     if (mixed) chain(mx_init<PRECOND>, -1);
-    else chain(cg64_init<PRECOND>, -1);
+    else if constexpr (!kSub) chain(cg64_init<PRECOND>, -1);
+    if (kSub) sub_apply(-1);
     for (int k = 0; k < iters; ++k) {
         if (mixed) {
             chain(mx_product<STORAGE>, 0);
             chain(mx_update<PRECOND>, 1);
             chain(mx_flush<false>, 2);
             chain(mx_residual<STORAGE>, 2);
-            chain(mx_reprecondition<PRECOND>, 3);
-        } else {
+            if constexpr (kSub) sub_apply(3);
+            else chain(mx_reprecondition<PRECOND>, 3);
+        } else if constexpr (!kSub) {  // the FP64 subdomain form is launch_separate_unrolled
             chain(cg64_product<STORAGE>, 0);
             chain(cg64_update<PRECOND>, 1);
             chain(cg64_direction, 2);
@@ -1266,6 +1394,20 @@ void launch_separate_unrolled(cudaStream_t stream, CgArgs* a, int blocks, const 
     }
 }
 
+// The subdomain arrays, and the apply kernel's launch shape.
+SeparateApply subdomain_args(Context& c, CgArgs& a) {
+    a.sub_dofs = c.sub_dofs;
+    a.sub_begin = c.sub_begin;
+    a.sub_fac = c.sub_fac_begin;
+    a.sub_factor = c.sub_factor;
+    a.sub_factor32 = c.sub_factor32;
+    SeparateApply ap{};
+    ap.subdomain = true;
+    ap.sub_grid = static_cast<int>(c.sub_count);
+    ap.sub_threads = std::max(32, (c.sub_max + 31) / 32 * 32);
+    return ap;
+}
+
 }  // namespace
 
 PcgResult finish_cg(Context& c, const SolveSetup& s);
@@ -1322,9 +1464,16 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         a.dhi = c.diag_hi;
         a.dlo = c.diag_lo;
     }
-    c.partials.ensure(static_cast<size_t>(kSlots) * kMaxReduce * blocks);
+    const bool sub = s.precond == LFGPU_PRECOND_SUBDOMAIN;
+    LF_REQUIRE(!sub || s.mixed, LFGPU_ERR_ARGUMENT, "the FP64 subdomain solve is run_pcg_separate");
+    SeparateApply ap{};
+    if (sub) ap = subdomain_args(c, a);
+    // Reduction partials: one per CTA of the widest reducing launch (the subdomain
+    // kernel runs a CTA per subdomain).
+    const int reducing = std::max(blocks, ap.sub_grid);
+    c.partials.ensure(static_cast<size_t>(kSlots) * kMaxReduce * reducing);
     a.partials = c.partials;
-    a.blocks = blocks;
+    a.blocks = reducing;
     c.cg_state.ensure(sizeof(CgState));
     a.st = reinterpret_cast<CgState*>(c.cg_state.p);
     a.status = c.status;
@@ -1343,7 +1492,13 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         const bool mx = s.mixed != 0;
         LF_CUDA(cudaEventRecord(c.ev_a, c.stream));
         EventTrail trail(c.stream, s.unrolled <= kTimedPasses);
-        if (csr && jac) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
+        if (sub && csr)
+            launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_SUBDOMAIN>(c.stream, &a, blocks, mx, s.unrolled, trail,
+                                                                        ap.sub_grid, ap.sub_threads);
+        else if (sub)
+            launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_SUBDOMAIN>(c.stream, &a, blocks, mx, s.unrolled, trail,
+                                                                        ap.sub_grid, ap.sub_threads);
+        else if (csr && jac) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
         else if (csr) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled, trail);
         else if (jac) launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
         else launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled, trail);
@@ -1362,7 +1517,11 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         else if (jac) build_fp64<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
         else build_fp64<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
     } else {
-        if (csr && jac) build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
+        if (sub && csr)
+            build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_SUBDOMAIN>(gb.graph, &a, blocks, ap.sub_grid, ap.sub_threads);
+        else if (sub)
+            build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_SUBDOMAIN>(gb.graph, &a, blocks, ap.sub_grid, ap.sub_threads);
+        else if (csr && jac) build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
         else if (csr) build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
         else if (jac) build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
         else build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
@@ -1390,8 +1549,14 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     // pass; subdomain block-Jacobi: one apply kernel in place of the two sweeps.
     if (s.precond == LFGPU_PRECOND_IC0)
         c.launches += (s.x0 ? 1 : 0) + 4 + 6 * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
-    else if (s.precond == LFGPU_PRECOND_SUBDOMAIN)
+    else if (s.precond == LFGPU_PRECOND_SUBDOMAIN && !s.mixed)
         c.launches += (s.x0 ? 1 : 0) + 3 + 5 * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
+    else if (s.precond == LFGPU_PRECOND_SUBDOMAIN)  // mixed: init + apply, then product, update, apply an
+                                                    // iteration, flush and residual per replacement, final flush
+        c.launches += 2 + (s.unrolled > 0 ? 5 * static_cast<i64>(s.unrolled)
+                                          : 3 * kBodyIterations * ((st.it + kBodyIterations - 1) / kBodyIterations) +
+                                                2 * st.refs) +
+                      1;
     else if (s.unrolled > 0)
         c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 5 : 3) +
                       (s.mixed ? 1 : 0);
@@ -1422,18 +1587,6 @@ void ic0_args(Context& c, CgArgs& a) {
     a.ic_chunks = c.ic0_misc.p + kIc0ForwardChunk;
 }
 
-// The subdomain arrays, and the apply kernel's launch shape.
-SeparateApply subdomain_args(Context& c, CgArgs& a) {
-    a.sub_dofs = c.sub_dofs;
-    a.sub_begin = c.sub_begin;
-    a.sub_fac = c.sub_fac_begin;
-    a.sub_factor = c.sub_factor;
-    SeparateApply ap{};
-    ap.subdomain = true;
-    ap.sub_grid = static_cast<int>(c.sub_count);
-    ap.sub_threads = std::max(32, (c.sub_max + 31) / 32 * 32);
-    return ap;
-}
 
 }  // namespace
 

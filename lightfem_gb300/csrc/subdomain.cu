@@ -195,6 +195,9 @@ void ensure_subdomains(Context& c) {
         static_cast<int>(c.n), c.rowptr, c.col, c.sub_owner, counters + 1);
     c.launches += c.sub_count > 0 ? 2 : 1;
     LF_CUDA(cudaGetLastError());
+    // The FP32 copy the mixed loop's block solves read.
+    c.sub_factor32.ensure(static_cast<size_t>(std::max<long long>(1, c.sub_factor_size)));
+    if (c.sub_factor_size > 0) launch_to_float(c, c.sub_factor, c.sub_factor32, c.sub_factor_size);
     unsigned long long h[2] = {0, 0};
     LF_CUDA(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
     check_status(c);

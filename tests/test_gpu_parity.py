@@ -228,7 +228,7 @@ def test_cfg2_full_size(native, golden_json, variant):
     """The 1000x1000 workload (2,004,002 DOFs, RCM) against the reference's own runs:
     FP64 PCG iteration count within 2, displacements within 1e-8; the mixed solve
     reaches the same true-residual target.  block64 is the reference's default
-    block preconditioner (64-node RCB subdomains, FP64 only)."""
+    block preconditioner (64-node RCB subdomains)."""
     ref = golden_json["cfg2"][variant]
     g = load_golden("cfg2")
     model = with_precond(indexed(mesh.workload(2)), *CFG2[variant])
@@ -240,7 +240,6 @@ def test_cfg2_full_size(native, golden_json, variant):
     assert abs(res.reaction[1::2].sum() - ref["R_y_sum"]) <= 1e-6
     if variant == "block64":
         assert res.solver.subdomains == 15657 and res.solver.capture_ratio == ref["capture_ratio"]
-        return
     mixed = with_precond(indexed(mesh.workload(2)), *CFG2[variant])
     mixed.settings.precision = "mixed"
     rm = LinearElasticSolver(retain_matrix=False, postprocess=False).solve(mixed)
@@ -377,9 +376,14 @@ def test_subdomain_solve_matches_oracle(native, oracle, storage, split):
     assert res.solver.subdomains == int(rep["stats"][0])
     assert res.solver.capture_ratio == rep["stats"][1]
     assert res.solver.preconditioner_setup_ms > 0.0 and res.solver.preconditioner_apply_ms > 0.0
+    # Mixed precision: FP32 block solves inside the FP32 loop, FP64 target on the
+    # true residual.
     model.settings.precision = "mixed"
-    with pytest.raises(RuntimeError, match="mixed precision supports"):
-        LinearElasticSolver().solve(model)
+    rm = LinearElasticSolver().solve(model)
+    assert rm.solver.converged and rm.solver.refinements >= 1
+    assert rm.solver.true_residual <= 1.001 * model.settings.tolerance * rm.solver.initial_residual
+    assert rel(rm.displacement, res.displacement) <= 1e-6
+    assert rm.solver.subdomains == int(rep["stats"][0])
 
 
 @pytest.mark.parametrize("name", ["grid6", "beam", "strain"])
@@ -404,7 +408,7 @@ def test_postprocess_fields(native, oracle, name):
 def test_ic0_rejects_mixed_precision(native):
     model = indexed(CASES["grid6"]())
     model.settings.preconditioner, model.settings.precision = "ic0", "mixed"
-    with pytest.raises(RuntimeError, match="mixed precision supports the jacobi and 2x2 block"):
+    with pytest.raises(RuntimeError, match="mixed precision supports the jacobi, block and subdomain"):
         LinearElasticSolver().solve(model)
 
 
