@@ -430,12 +430,15 @@ def run_ours(args) -> int:
 
     # other variants, one solve each (device time of the solve alone)
     variants = []
+    ctx.set_subdomains(64, "rcb")  # the reference's default block setting, for the "subdomain" variant
     for prec, st, pc, pers in (("mixed", "bsr", "block", False), ("mixed", "csr", "jacobi", False),
                                ("fp64", "csr", "jacobi", False), ("fp64", "bsr", "block", False),
+                               ("mixed", "bsr", "subdomain", False),
                                ("mixed", "bsr", "jacobi", True), ("fp64", "csr", "jacobi", True)):
         try:
             ms, r = step(opts(prec, st, pc, pers))
             variants.append({"precision": prec, "storage": st, "preconditioner": pc,
+                             **({"subdomain_nodes": 64, "subdomain_split": "rcb"} if pc == "subdomain" else {}),
                              "loop": "persistent" if pers else "graph", "step_ms": round(ms, 2),
                              "solve_ms": round(r.solve_ms, 2), "iterations": r.iterations,
                              "refinements": r.refinements, "true_residual_rel": r.true_residual / r.initial_residual})

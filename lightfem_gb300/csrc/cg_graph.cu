@@ -254,31 +254,44 @@ __device__ __forceinline__ void csr64_rows(const CgArgs& a, const G& g, Out&& ou
 // block; even lanes sum the top row, odd lanes the bottom row.
 template <typename G, typename Out>
 __device__ __forceinline__ void bsr64_rows(const CgArgs& a, const G& g, Out&& out) {
-    const int lane = threadIdx.x & 31;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const int l8 = lane & 7, half = l8 & 1, pair = l8 >> 1;
-    for (int base = warp * 4; base < a.nb; base += nwarps * 4) {
-        const int node = base + (lane >> 3);
-        double s = 0.0;
-        if (node < a.nb) {
+    // A quarter warp per block row, whole 2x2 blocks per lane (two 16-byte
+    // loads), three blocks in flight per lane: the nine blocks of an interior
+    // node in one round.  Fused multiply-adds only: GB300's FP64 pipe is the bound.
+    rows_by_quad(a.nb, [&](bool act, int node, int sub) {
+        double s0 = 0.0, s1 = 0.0;
+        if (act) {
             const int b = __ldg(a.brow + node), e = __ldg(a.brow + node + 1);
-            for (int k = b + pair; k < e; k += 8) {  // two blocks in flight per lane
-                const bool two = k + 4 < e;
-                const double2 v0 = ld_stream(a.bval64 + 2 * static_cast<size_t>(k) + half);
-                const double2 v1 = two ? ld_stream(a.bval64 + 2 * static_cast<size_t>(k + 4) + half)
-                                       : make_double2(0.0, 0.0);
-                const int c0 = ld_stream(a.bcol + k), c1 = two ? ld_stream(a.bcol + k + 4) : c0;
-                const double2 x0 = g(c0), x1 = g(c1);
-                s += v0.x * x0.x + v0.y * x0.y;
-                s += v1.x * x1.x + v1.y * x1.y;
+            for (int k = b + sub; k < e; k += 12) {
+                const bool t1 = k + 4 < e, t2 = k + 8 < e;
+                const double2 zero = make_double2(0.0, 0.0);
+                const int c0 = ld_stream(a.bcol + k);
+                const int c1 = t1 ? ld_stream(a.bcol + k + 4) : c0;
+                const int c2 = t2 ? ld_stream(a.bcol + k + 8) : c0;
+                const double2 u0 = ld_stream(a.bval64 + 2 * static_cast<size_t>(k));
+                const double2 w0 = ld_stream(a.bval64 + 2 * static_cast<size_t>(k) + 1);
+                const double2 u1 = t1 ? ld_stream(a.bval64 + 2 * static_cast<size_t>(k + 4)) : zero;
+                const double2 w1 = t1 ? ld_stream(a.bval64 + 2 * static_cast<size_t>(k + 4) + 1) : zero;
+                const double2 u2 = t2 ? ld_stream(a.bval64 + 2 * static_cast<size_t>(k + 8)) : zero;
+                const double2 w2 = t2 ? ld_stream(a.bval64 + 2 * static_cast<size_t>(k + 8) + 1) : zero;
+                const double2 x0 = g(c0), x1 = g(c1), x2 = g(c2);
+                s0 = fma(u0.x, x0.x, s0);
+                s0 = fma(u0.y, x0.y, s0);
+                s1 = fma(w0.x, x0.x, s1);
+                s1 = fma(w0.y, x0.y, s1);
+                s0 = fma(u1.x, x1.x, s0);
+                s0 = fma(u1.y, x1.y, s0);
+                s1 = fma(w1.x, x1.x, s1);
+                s1 = fma(w1.y, x1.y, s1);
+                s0 = fma(u2.x, x2.x, s0);
+                s0 = fma(u2.y, x2.y, s0);
+                s1 = fma(w2.x, x2.x, s1);
+                s1 = fma(w2.y, x2.y, s1);
             }
         }
-        s += __shfl_xor_sync(0xffffffffu, s, 2);
-        s += __shfl_xor_sync(0xffffffffu, s, 4);
-        const double s1 = __shfl_down_sync(0xffffffffu, s, 1);
-        if (node < a.nb && l8 == 0) out(node, make_double2(s, s1));
-    }
+        s0 = quad_sum(s0);
+        s1 = quad_sum(s1);
+        if (act && sub == 0) out(node, make_double2(s0, s1));
+    });
 }
 
 // FP32 BSR block rows, quarter warp per block row (one 16-byte block per lane).

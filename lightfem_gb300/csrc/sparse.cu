@@ -134,8 +134,10 @@ __global__ void __launch_bounds__(kThreads) spmv_bsr64_kernel(int nb, const int*
             const double2 v1 = two ? ld_stream(bval + 2 * static_cast<size_t>(k + 4) + half) : make_double2(0.0, 0.0);
             const int c0 = ld_stream(bcol + k), c1 = two ? ld_stream(bcol + k + 4) : c0;
             const double2 x0 = x[c0], x1 = x[c1];
-            s += v0.x * x0.x + v0.y * x0.y;
-            s += v1.x * x1.x + v1.y * x1.y;
+            s = fma(v0.x, x0.x, s);  // fused: GB300's FP64 pipe is the bound
+            s = fma(v0.y, x0.y, s);
+            s = fma(v1.x, x1.x, s);
+            s = fma(v1.y, x1.y, s);
         }
     }
     s += __shfl_xor_sync(0xffffffffu, s, 2);

@@ -128,3 +128,25 @@ def test_gradients_match_central_differences(cfg4):
     for got, want in ((np.array(fd_c), dc[elements]), (np.array(fd_t), dtip[elements])):
         assert np.all(np.abs(got - want) <= 5e-3 * np.abs(want).max())
         assert rel(got, want) <= 1e-2
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_subdomain_preconditioner_gradient(cfg4, cpu_reference, precision):
+    """The forward and adjoint solves with the reference's default block
+    preconditioner (64-node RCB subdomains) give the same tip-displacement
+    gradient as the CPU FP64 reference."""
+    from lightfem_gb300.adjoint import ElasticProblem, displacements
+    problem, tip = cfg4
+    model = problem.model.copy()
+    model.settings.reordering = "none"  # the problem's model is already reordered
+    model.settings.preconditioner, model.settings.subdomain_nodes, model.settings.subdomain_split = "block", 64, "rcb"
+    sub = ElasticProblem(model, precision=precision, tolerance=TOL, max_iterations=200000)
+    try:
+        young = torch.tensor(sub.young0, dtype=torch.float64, requires_grad=True)
+        u = displacements(young, sub)
+        assert rel(u.detach().numpy(), cpu_reference["u"]) <= 1e-7
+        u[tip].backward()
+        assert sub.report.subdomains > 0 and sub.adjoint_report.converged
+        assert rel(young.grad.numpy(), cpu_reference["dtip"]) <= 1e-6
+    finally:
+        sub.close()
