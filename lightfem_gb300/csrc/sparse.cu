@@ -120,30 +120,45 @@ __global__ void __launch_bounds__(kThreads) spmv_bsr64_kernel(int nb, const int*
                                                               const int* __restrict__ bcol,
                                                               const double2* __restrict__ bval,
                                                               const double2* __restrict__ x, double2* __restrict__ y) {
-    // 8 lanes per block row; a lane pair reads the two 16-byte halves of one block,
-    // so consecutive lanes read consecutive 16-byte chunks.  Even lanes sum the top
-    // row, odd lanes the bottom row.
-    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
-    const int l8 = threadIdx.x & 7, half = l8 & 1, pair = l8 >> 1;
-    double s = 0.0;
+    // A quarter warp per block row, whole 2x2 blocks per lane (top and bottom
+    // rows as two 16-byte loads), three blocks in flight per lane, fused
+    // multiply-adds only: GB300's FP64 pipe is the bound.
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+    const int q = threadIdx.x & 3;
+    double s0 = 0.0, s1 = 0.0;
     if (row < nb) {
         const int b = __ldg(brow + row), e = __ldg(brow + row + 1);
-        for (int k = b + pair; k < e; k += 8) {  // two blocks in flight per lane
-            const bool two = k + 4 < e;
-            const double2 v0 = ld_stream(bval + 2 * static_cast<size_t>(k) + half);
-            const double2 v1 = two ? ld_stream(bval + 2 * static_cast<size_t>(k + 4) + half) : make_double2(0.0, 0.0);
-            const int c0 = ld_stream(bcol + k), c1 = two ? ld_stream(bcol + k + 4) : c0;
-            const double2 x0 = x[c0], x1 = x[c1];
-            s = fma(v0.x, x0.x, s);  // fused: GB300's FP64 pipe is the bound
-            s = fma(v0.y, x0.y, s);
-            s = fma(v1.x, x1.x, s);
-            s = fma(v1.y, x1.y, s);
+        for (int k = b + q; k < e; k += 12) {
+            const double2 zero = make_double2(0.0, 0.0);
+            const bool t1 = k + 4 < e, t2 = k + 8 < e;
+            const int c0 = ld_stream(bcol + k), c1 = t1 ? ld_stream(bcol + k + 4) : c0,
+                      c2 = t2 ? ld_stream(bcol + k + 8) : c0;
+            const double2 u0 = ld_stream(bval + 2 * static_cast<size_t>(k));
+            const double2 w0 = ld_stream(bval + 2 * static_cast<size_t>(k) + 1);
+            const double2 u1 = t1 ? ld_stream(bval + 2 * static_cast<size_t>(k + 4)) : zero;
+            const double2 w1 = t1 ? ld_stream(bval + 2 * static_cast<size_t>(k + 4) + 1) : zero;
+            const double2 u2 = t2 ? ld_stream(bval + 2 * static_cast<size_t>(k + 8)) : zero;
+            const double2 w2 = t2 ? ld_stream(bval + 2 * static_cast<size_t>(k + 8) + 1) : zero;
+            const double2 x0 = x[c0], x1 = x[c1], x2 = x[c2];
+            s0 = fma(u0.x, x0.x, s0);
+            s0 = fma(u0.y, x0.y, s0);
+            s1 = fma(w0.x, x0.x, s1);
+            s1 = fma(w0.y, x0.y, s1);
+            s0 = fma(u1.x, x1.x, s0);
+            s0 = fma(u1.y, x1.y, s0);
+            s1 = fma(w1.x, x1.x, s1);
+            s1 = fma(w1.y, x1.y, s1);
+            s0 = fma(u2.x, x2.x, s0);
+            s0 = fma(u2.y, x2.y, s0);
+            s1 = fma(w2.x, x2.x, s1);
+            s1 = fma(w2.y, x2.y, s1);
         }
     }
-    s += __shfl_xor_sync(0xffffffffu, s, 2);
-    s += __shfl_xor_sync(0xffffffffu, s, 4);
-    const double s1 = __shfl_down_sync(0xffffffffu, s, 1);
-    if (row < nb && l8 == 0) y[row] = make_double2(s, s1);
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
+    s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+    if (row < nb && q == 0) y[row] = make_double2(s0, s1);
 }
 
 __global__ void __launch_bounds__(kThreads) spmv_bsr32_kernel(int nb, const int* __restrict__ brow,
@@ -438,7 +453,7 @@ void launch_spmv_csr32(Context& c, const float* val, const float* x, float* y) {
 
 void launch_spmv_bsr64(Context& c, const double* x, double* y) {
     const int nb = static_cast<int>(c.n / 2);
-    spmv_bsr64_kernel<<<grid_for(8LL * nb, kThreads), kThreads, 0, c.stream>>>(
+    spmv_bsr64_kernel<<<grid_for(4LL * nb, kThreads), kThreads, 0, c.stream>>>(
         nb, c.brow, c.bcol, reinterpret_cast<const double2*>(c.bval64.p), reinterpret_cast<const double2*>(x),
         reinterpret_cast<double2*>(y));
     c.launches += 1;
