@@ -598,7 +598,8 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
             r.preconditioner_apply_ms = apply_ms;
         } else if (o->preconditioner == LFGPU_PRECOND_SUBDOMAIN) {
             LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
-            ensure_subdomains(*h);
+            if (s.mixed) ensure_subdomain_inverse(*h);  // factor, then the FP32 block inverses
+            else ensure_subdomains(*h);
             LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
             r.preconditioner_setup_ms = elapsed_ms(*h);
             if (o->storage == LFGPU_STORAGE_BSR) ensure_bsr(*h);
@@ -904,6 +905,7 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
             PcgResult res;
             if (o->preconditioner == LFGPU_PRECOND_IC0 || o->preconditioner == LFGPU_PRECOND_SUBDOMAIN) {
                 if (o->preconditioner == LFGPU_PRECOND_IC0) ensure_ic0(*h);
+                else if (s.mixed) ensure_subdomain_inverse(*h);
                 else ensure_subdomains(*h);
                 res = s.mixed ? run_cg_graph(*h, s, &ms) : run_pcg_separate(*h, s, &ms, &apply_ms);
             } else {

@@ -84,7 +84,8 @@ struct CgArgs {
     const int* sub_begin;
     const long long* sub_fac;      // packed lower factor offset of each subdomain
     const double* sub_factor;
-    const float* sub_factor32;     // FP32 copy for the mixed loop
+    const float* sub_inv32;        // mixed loop: block inverses, FP32 D x D squares
+    const long long* sub_sq;       // offset of each subdomain's square
     int blocks;
     CgState* st;
     DeviceStatus* status;
@@ -1059,81 +1060,42 @@ __global__ void __launch_bounds__(LFGPU_SUBDOMAIN_MAX_DOFS) subdomain_apply(CgAr
     if (mine) a.z[dof] = x;
 }
 
-// The mixed loop's application of the subdomain preconditioner: the same block
-// solves in FP32 (an FP32 copy of the factor, fused multiply-adds) on r32, z
-// into the (z, p) copy the next product reads, and r.z.  Its reduction sets rho
-// and beta: after mx_init the first rho (r0.z0 > 0 or "positive initial
-// preconditioned residual"), in the loop beta = r.z / rho, or 0 after a residual
-// replacement in restart mode.
+// The mixed loop's application of the subdomain preconditioner: z = M_s^-1 r on
+// every subdomain with the block inverses (FP32 D x D squares, built in FP64 by
+// subdomain.cu), on r32; z into the (z, p) copy the next product reads, and r.z.
+// Its reduction sets rho and beta: after mx_init the first rho (r0.z0 > 0 or
+// "positive initial preconditioned residual"), in the loop beta = r.z / rho, or
+// 0 after a residual replacement in restart mode.
 //
-// In FP32 a step is a few cycles, so a CTA barrier per unknown would dominate.
-// The solves run in tiles of 32 rows instead.  The warp that owns the diagonal
-// tile resolves its 32 unknowns one by one with shuffles.  After one barrier,
-// every later row subtracts the tile's 32 terms.  Each row still subtracts its
-// terms in ascending order forward and descending order backward.
+// A dense product has no dependency chain (the triangular solves of the FP64
+// form need one barrier per unknown).  Thread i sums entry i of every row of the
+// symmetric inverse, so a warp's loads are consecutive.
 __global__ void __launch_bounds__(LFGPU_SUBDOMAIN_MAX_DOFS) mx_sub_apply(CgArgs a) {
     if (a.st->done) return;
-    __shared__ float v[LFGPU_SUBDOMAIN_MAX_DOFS];
-    const int s = blockIdx.x, i = threadIdx.x, lane = i & 31, wid = i >> 5;
+    __shared__ float rs[LFGPU_SUBDOMAIN_MAX_DOFS];
+    const int s = blockIdx.x, i = threadIdx.x;
     const int begin = a.sub_begin[s], D = a.sub_begin[s + 1] - begin;
-    const float* __restrict__ f = a.sub_factor32 + a.sub_fac[s];
+    const float* __restrict__ A = a.sub_inv32 + a.sub_sq[s];
     const bool mine = i < D;
     const int dof = mine ? a.sub_dofs[begin + i] : 0;
-    const float* __restrict__ row = f + static_cast<long long>(i) * (i + 1) / 2;  // row i of L
     const float r = mine ? a.r32[dof] : 0.f;
-    const int tiles = (D + 31) / 32;
-    float acc = r;
-    for (int t = 0; t < tiles; ++t) {  // forward: L y = r
-        const int t0 = 32 * t, cnt = min(32, D - t0);
-        if (wid == t) {
-            float dg[32];  // this row's entries in the tile (the reciprocal pivot at u == lane), loaded first
-#pragma unroll
-            for (int u = 0; u < 32; ++u) dg[u] = (mine && u <= lane && u < cnt) ? row[t0 + u] : 0.f;
-#pragma unroll
-            for (int u = 0; u < 32; ++u) {
-                if (u < cnt) {
-                    float vj = lane == u ? acc * dg[u] : 0.f;
-                    vj = __shfl_sync(0xffffffffu, vj, u);
-                    if (mine && lane > u) acc = fmaf(-dg[u], vj, acc);
-                    if (lane == u) v[t0 + u] = vj;
-                }
-            }
-        }
-        __syncthreads();
-        if (mine && wid > t) {
-#pragma unroll 8
-            for (int u = 0; u < cnt; ++u) acc = fmaf(-row[t0 + u], v[t0 + u], acc);
-        }
-    }
-    acc = mine ? v[i] : 0.f;  // this thread's own y
+    rs[i] = r;
+    __syncthreads();
     float x = 0.f;
-    for (int t = tiles - 1; t >= 0; --t) {  // backward: L^T z = y
-        const int t0 = 32 * t, cnt = min(32, D - t0);
-        if (wid == t) {
-            float dg[32];  // L(k, i) for the tile's rows k >= i (the reciprocal pivot at k == i), loaded first
+    if (mine) {
+        // Eight loads in flight per thread: the stream is latency-bound otherwise.
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        const float* __restrict__ col = A + i;
+        int j = 0;
+        for (; j + 7 < D; j += 8) {
+            float t[8];
 #pragma unroll
-            for (int u = 0; u < 32; ++u) {
-                const int k = t0 + u;
-                dg[u] = (u >= lane && u < cnt) ? f[static_cast<long long>(k) * (k + 1) / 2 + i] : 0.f;
-            }
+            for (int u = 0; u < 8; ++u) t[u] = __ldg(col + static_cast<long long>(j + u) * D);
 #pragma unroll
-            for (int u = 31; u >= 0; --u) {
-                if (u < cnt) {
-                    float xk = lane == u ? acc * dg[u] : 0.f;
-                    xk = __shfl_sync(0xffffffffu, xk, u);
-                    if (lane < u) acc = fmaf(-dg[u], xk, acc);
-                    if (lane == u) v[t0 + u] = x = xk;
-                }
-            }
+            for (int u = 0; u < 8; ++u) acc[u & 3] = fmaf(t[u], rs[j + u], acc[u & 3]);
         }
-        __syncthreads();
-        if (mine && wid < t) {
-#pragma unroll 8
-            for (int u = cnt - 1; u >= 0; --u) {
-                const int k = t0 + u;
-                acc = fmaf(-f[static_cast<long long>(k) * (k + 1) / 2 + i], v[k], acc);
-            }
-        }
+        for (; j < D; ++j) acc[0] = fmaf(__ldg(col + static_cast<long long>(j) * D), rs[j], acc[0]);
+        x = (acc[0] + acc[1]) + (acc[2] + acc[3]);
     }
     FloatPair rz;
     if (mine) {
@@ -1413,7 +1375,8 @@ SeparateApply subdomain_args(Context& c, CgArgs& a) {
     a.sub_begin = c.sub_begin;
     a.sub_fac = c.sub_fac_begin;
     a.sub_factor = c.sub_factor;
-    a.sub_factor32 = c.sub_factor32;
+    a.sub_inv32 = c.sub_inv32;
+    a.sub_sq = c.sub_sq_begin;
     SeparateApply ap{};
     ap.subdomain = true;
     ap.sub_grid = static_cast<int>(c.sub_count);
@@ -1480,7 +1443,10 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
     const bool sub = s.precond == LFGPU_PRECOND_SUBDOMAIN;
     LF_REQUIRE(!sub || s.mixed, LFGPU_ERR_ARGUMENT, "the FP64 subdomain solve is run_pcg_separate");
     SeparateApply ap{};
-    if (sub) ap = subdomain_args(c, a);
+    if (sub) {
+        ensure_subdomain_inverse(c);  // no-op when the solve's setup built it
+        ap = subdomain_args(c, a);
+    }
     // Reduction partials: one per CTA of the widest reducing launch (the subdomain
     // kernel runs a CTA per subdomain).
     const int reducing = std::max(blocks, ap.sub_grid);

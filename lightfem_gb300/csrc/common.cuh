@@ -205,8 +205,10 @@ struct Context {
     Buf<int> sub_dofs, sub_begin, sub_owner, sub_local;  // DOFs by subdomain; per DOF: subdomain, slot
     Buf<long long> sub_fac_begin;
     Buf<double> sub_factor;
-    Buf<float> sub_factor32;  // FP32 copy for the mixed loop
-    i64 sub_count = 0, sub_degenerate = 0, sub_factor_size = 0;
+    Buf<float> sub_inv32;     // mixed loop: each block's inverse, D x D in FP32 (per K version)
+    Buf<long long> sub_sq_begin;  // offsets of D x D scratch per subdomain (the inverse's FP64 work)
+    unsigned long long sub_inv_version = ~0ull;
+    i64 sub_count = 0, sub_degenerate = 0, sub_factor_size = 0, sub_sq_size = 0;
     int sub_max = 0;  // DOFs of the largest subdomain
     double sub_capture = 0.0;
 

@@ -54,6 +54,8 @@ void launch_precond_apply(Context& c, int precond, const double* r, double* z);
 // subdomain.cu: subdomain block-Jacobi split (per mesh and setting) and factor
 // (per K version)
 void ensure_subdomains(Context& c);
+// Each block's inverse in FP32 (a D x D square) for the mixed loop, per K version.
+void ensure_subdomain_inverse(Context& c);
 
 // ic0.cu: IC(0) factor of the constrained K on its own pattern (built per K version)
 enum Ic0Slot {

@@ -110,6 +110,43 @@ __global__ void __launch_bounds__(kCaptureThreads) subdomain_capture_kernel(int 
     if ((threadIdx.x & 31) == 0 && count) atomicAdd(inside, count);
 }
 
+// Each block's inverse M^-1 = (L L^T)^-1 for the mixed loop: thread j solves
+// L L^T x = e_j in FP64 with the packed factor (forward, then backward in place,
+// x in the FP64 scratch `work`, laid out k-major so that the threads' accesses
+// coalesce), and stores the whole inverse in FP32 as a D x D square (one
+// subdomain after another at the scratch's offsets).  Forward, the lanes of a warp
+// read neighbouring entries of one factor row; backward, every thread reads the
+// same entry (a broadcast).
+__global__ void __launch_bounds__(LFGPU_SUBDOMAIN_MAX_DOFS) subdomain_inverse_kernel(
+    const int* __restrict__ sub_begin, const long long* __restrict__ fac_begin,
+    const long long* __restrict__ sq_begin, const double* __restrict__ factor, double* __restrict__ work,
+    float* __restrict__ inv) {
+    const int s = blockIdx.x, j = threadIdx.x;
+    const int D = sub_begin[s + 1] - sub_begin[s];
+    const double* L = factor + fac_begin[s];
+    double* x = work + sq_begin[s];  // x[k * D + j]: entry k of thread j's column
+    const bool mine = j < D;
+    for (int i = 0; i < D; ++i) {  // forward: L y = e_j (y_k = 0 for k < j)
+        const double* li = L + static_cast<long long>(i) * (i + 1) / 2;
+        double acc = (i == j) ? 1.0 : 0.0;
+        if (i > j)
+            for (int k = j; k < i; ++k) acc = fma(-li[k], x[static_cast<long long>(k) * D + j], acc);
+        if (mine) x[static_cast<long long>(i) * D + j] = i < j ? 0.0 : acc * li[i];  // li[i]: reciprocal pivot
+    }
+    for (int i = D - 1; i >= 0; --i) {  // backward: L^T x = y, in place
+        double acc = mine ? x[static_cast<long long>(i) * D + j] : 0.0;
+        for (int k = i + 1; k < D; ++k)
+            acc = fma(-L[static_cast<long long>(k) * (k + 1) / 2 + i], mine ? x[static_cast<long long>(k) * D + j] : 0.0,
+                      acc);
+        if (mine) x[static_cast<long long>(i) * D + j] = acc * L[static_cast<long long>(i) * (i + 1) / 2 + i];
+    }
+    // The whole square in FP32, in the scratch's layout: entry (k, j) at k D + j,
+    // which by symmetry is also entry (j, k).
+    float* out = inv + sq_begin[s];
+    for (int k = 0; k < D; ++k)
+        if (mine) out[static_cast<long long>(k) * D + j] = static_cast<float>(x[static_cast<long long>(k) * D + j]);
+}
+
 // The split and the per-subdomain DOF lists, rebuilt when the mesh or the
 // requested split changes.
 void build_split(Context& c) {
@@ -147,16 +184,18 @@ void build_split(Context& c) {
         dofs[static_cast<size_t>(slot)] = static_cast<int>(d);
         local[static_cast<size_t>(d)] = slot - begin[static_cast<size_t>(o)];
     }
-    std::vector<long long> fac(static_cast<size_t>(S) + 1, 0);
+    std::vector<long long> fac(static_cast<size_t>(S) + 1, 0), sq(static_cast<size_t>(S) + 1, 0);
     for (i64 k = 0; k < S; ++k) {
         const long long size = begin[static_cast<size_t>(k) + 1] - begin[static_cast<size_t>(k)];
         fac[static_cast<size_t>(k) + 1] = fac[static_cast<size_t>(k)] + size * (size + 1) / 2;
+        sq[static_cast<size_t>(k) + 1] = sq[static_cast<size_t>(k)] + size * size;
     }
     c.sub_dofs.ensure(static_cast<size_t>(n));
     c.sub_owner.ensure(static_cast<size_t>(n));
     c.sub_local.ensure(static_cast<size_t>(n));
     c.sub_begin.ensure(static_cast<size_t>(S) + 1);
     c.sub_fac_begin.ensure(static_cast<size_t>(S) + 1);
+    c.sub_sq_begin.ensure(static_cast<size_t>(S) + 1);
     LF_CUDA(cudaMemcpyAsync(c.sub_dofs.p, dofs.data(), sizeof(int) * dofs.size(), cudaMemcpyHostToDevice, c.stream));
     LF_CUDA(cudaMemcpyAsync(c.sub_owner.p, owner.data(), sizeof(int) * owner.size(), cudaMemcpyHostToDevice,
                             c.stream));
@@ -166,6 +205,9 @@ void build_split(Context& c) {
                             c.stream));
     LF_CUDA(cudaMemcpyAsync(c.sub_fac_begin.p, fac.data(), sizeof(long long) * fac.size(), cudaMemcpyHostToDevice,
                             c.stream));
+    LF_CUDA(cudaMemcpyAsync(c.sub_sq_begin.p, sq.data(), sizeof(long long) * sq.size(), cudaMemcpyHostToDevice,
+                            c.stream));
+    c.sub_sq_size = sq.back();
     LF_CUDA(cudaStreamSynchronize(c.stream));  // the host vectors end with this function
     c.sub_count = S;
     c.sub_max = largest;
@@ -195,15 +237,31 @@ void ensure_subdomains(Context& c) {
         static_cast<int>(c.n), c.rowptr, c.col, c.sub_owner, counters + 1);
     c.launches += c.sub_count > 0 ? 2 : 1;
     LF_CUDA(cudaGetLastError());
-    // The FP32 copy the mixed loop's block solves read.
-    c.sub_factor32.ensure(static_cast<size_t>(std::max<long long>(1, c.sub_factor_size)));
-    if (c.sub_factor_size > 0) launch_to_float(c, c.sub_factor, c.sub_factor32, c.sub_factor_size);
     unsigned long long h[2] = {0, 0};
     LF_CUDA(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
     check_status(c);
     c.sub_degenerate = static_cast<i64>(h[0]);
     c.sub_capture = c.nnz > 0 ? static_cast<double>(h[1]) / static_cast<double>(c.nnz) : 0.0;
     c.sub_k_version = c.k_version;
+}
+
+void ensure_subdomain_inverse(Context& c) {
+    ensure_subdomains(c);
+    if (c.sub_inv_version == c.k_version) return;
+    c.sub_inv32.ensure(static_cast<size_t>(std::max<long long>(1, c.sub_sq_size)));
+    if (c.sub_count > 0) {
+        // FP64 scratch for the columns, released again: it is twice the factor's size.
+        Buf<double> work;
+        work.ensure(static_cast<size_t>(std::max<long long>(1, c.sub_sq_size)));
+        const int threads = std::max(32, (c.sub_max + 31) / 32 * 32);
+        subdomain_inverse_kernel<<<static_cast<unsigned>(c.sub_count), threads, 0, c.stream>>>(
+            c.sub_begin, c.sub_fac_begin, c.sub_sq_begin, c.sub_factor, work, c.sub_inv32);
+        c.launches += 1;
+        LF_CUDA(cudaGetLastError());
+        LF_CUDA(cudaStreamSynchronize(c.stream));
+        work.release();
+    }
+    c.sub_inv_version = c.k_version;
 }
 
 }  // namespace lfgpu
