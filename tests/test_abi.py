@@ -73,3 +73,17 @@ def test_host_subdomains_match_oracle(native, oracle):
                 want, n_want = oracle.subdomain_split(model.xy, per, split)
                 assert n_got == n_want
                 np.testing.assert_array_equal(got, want)
+
+
+def test_host_subdomains_rejects_bad_arguments(native):
+    import ctypes
+    import pytest
+    lib = native.library()
+    xy = np.zeros((4, 2))
+    owner = np.empty(4, np.uint32)
+    count = ctypes.c_int64()
+    for per, split in ((0, 0), (-3, 1), (4, 2), (4, -1)):
+        rc = lib.lfgpu_host_subdomains(4, xy.ctypes.data, per, split, owner.ctypes.data, ctypes.byref(count))
+        assert rc == native.ERR_ARGUMENT, (per, split)
+    with pytest.raises(KeyError):
+        native.host_subdomains(xy, 4, "metis")
