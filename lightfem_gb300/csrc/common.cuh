@@ -34,11 +34,15 @@ struct Error {
         if (!(cond)) throw ::lfgpu::Error{(code), (msg)}; \
     } while (0)
 
-// Device buffer that grows on demand and is released with the handle.
+// Device buffer that grows on demand and is released with its owner (the handle).
 template <typename T>
 struct Buf {
     T* p = nullptr;
     size_t count = 0;
+    Buf() = default;
+    Buf(const Buf&) = delete;
+    Buf& operator=(const Buf&) = delete;
+    ~Buf() { release(); }  // every buffer of a handle goes with it, whatever lfgpu_destroy lists
     void ensure(size_t n) {
         if (n <= count && p != nullptr) return;
         release();
