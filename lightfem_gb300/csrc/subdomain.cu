@@ -215,7 +215,8 @@ void build_split(Context& c) {
     c.sub_mesh_version = c.mesh_version;
     c.sub_nodes_built = c.sub_nodes;
     c.sub_split_built = c.sub_split;
-    c.sub_k_version = ~0ull;
+    c.sub_k_version = ~0ull;    // the factors and the mixed loop's inverses follow the new split
+    c.sub_inv_version = ~0ull;
 }
 
 }  // namespace

@@ -386,6 +386,33 @@ def test_subdomain_solve_matches_oracle(native, oracle, storage, split):
     assert rm.solver.subdomains == int(rep["stats"][0])
 
 
+def test_subdomain_split_change_rebuilds_blocks(native):
+    """Changing the split on a handle whose K is unchanged rebuilds the factors and
+    the mixed loop's block inverses: the second solve equals a fresh handle's."""
+    model = indexed(CASES["beam"]())
+
+    def solve(ctx, nodes, split):
+        ctx.set_subdomains(nodes, split)
+        opts = ctx.options(1e-10, 20000, "bsr", "subdomain", "mixed")
+        u, rep = ctx.solve(opts)
+        assert rep.converged
+        return u, rep
+
+    ctx = native.Context(0)
+    upload_model(ctx, model)
+    ctx.assemble("coloring")
+    ctx.apply_dirichlet()
+    solve(ctx, 64, "rcb")
+    u2, rep2 = solve(ctx, 16, "chunk")
+    fresh = native.Context(0)
+    upload_model(fresh, model)
+    fresh.assemble("coloring")
+    fresh.apply_dirichlet()
+    u3, rep3 = solve(fresh, 16, "chunk")
+    assert rep2.subdomains == rep3.subdomains and rep2.iterations == rep3.iterations
+    np.testing.assert_array_equal(u2, u3)
+
+
 @pytest.mark.parametrize("name", ["grid6", "beam", "strain"])
 def test_postprocess_fields(native, oracle, name):
     """Element fields and smoothed nodal stress on the device: bit for bit the
