@@ -647,7 +647,7 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
         r.matrix_bytes_per_matvec =
             o->storage == LFGPU_STORAGE_BSR
                 ? h->nblocks * (s.mixed ? 4 * 4 + (h->bcol16_ok ? 2 : 4) : 4 * 8 + 4)
-                : h->nnz * ((s.mixed ? 4 : 8) + 4);
+                : h->nnz * (s.mixed ? 4 + (h->col16_ok ? 2 : 4) : 8 + 4);
         // True residual ||f - K u|| in FP64.
         Buf<double>& tmp = h->v64[0];
         tmp.ensure(h->n);

@@ -51,6 +51,7 @@ struct CgArgs {
     const int* brow;
     const int* bcol;
     const short* bcol16;           // FP32 BSR: columns as offsets from the block row, or nullptr
+    const short* col16;            // FP32 CSR: columns as offsets from the row, or nullptr
     const double2* bval64;
     const float4* bval32;
     const float* dhi;
@@ -344,7 +345,9 @@ __device__ __forceinline__ void csr32_rows(const CgArgs& a, const G& g, Out&& ou
 #pragma unroll
                 for (int j = 0; j < 5; ++j) {
                     const bool on = k + 4 * j < e;
-                    c[j] = on ? ld_stream(a.col + k + 4 * j) : ld_stream(a.col + k);
+                    const int kk = on ? k + 4 * j : k;
+                    // Columns as 16-bit offsets from the row when they fit (half the bytes).
+                    c[j] = a.col16 ? row + ld_stream(a.col16 + kk) : ld_stream(a.col + kk);
                     v[j] = on ? ld_stream(a.K32 + k + 4 * j) : 0.f;
                 }
                 float x[5];
@@ -1436,6 +1439,7 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         } else {
             ensure_csr32(c);
             a.K32 = c.K32;
+            a.col16 = c.col16_ok ? c.col16.p : nullptr;
         }
         a.dhi = c.diag_hi;
         a.dlo = c.diag_lo;

@@ -146,6 +146,8 @@ struct Context {
     Buf<short> bcol16;      // FP32 BSR columns as offsets from the block row, when all fit in 16 bits
     bool bcol16_ok = false;
     Buf<float> K32;
+    Buf<short> col16;       // FP32 CSR columns as offsets from the row, when all fit in 16 bits
+    bool col16_ok = false;
     i64 nblocks = 0;
     unsigned long long bsr_version = ~0ull, k32_version = ~0ull, b32_version = ~0ull;
     double last_convert_ms = 0.0;

@@ -564,6 +564,22 @@ void ensure_bsr32(Context& c) {
     c.b32_version = c.k_version;
 }
 
+// Columns as 16-bit offsets from the row (the FP32 CSR product's column stream
+// at half the bytes); *wide is set when an offset does not fit.
+__global__ void csr_offsets_kernel(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                   short* __restrict__ off, int* __restrict__ wide) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n) return;
+    for (int k = rowptr[row]; k < rowptr[row + 1]; ++k) {
+        const int d = col[k] - row;
+        if (d < -32768 || d > 32767) {
+            atomicOr(wide, 1);
+            return;
+        }
+        off[k] = static_cast<short>(d);
+    }
+}
+
 void ensure_csr32(Context& c) {
     if (c.k32_version == c.k_version) return;
     c.K32.ensure(c.nnz);
@@ -573,7 +589,18 @@ void ensure_csr32(Context& c) {
                                                                                c.col, c.K, c.K32, c.diag_hi,
                                                                                c.diag_lo);
     c.launches += 1;
+    c.col16.ensure(static_cast<size_t>(c.nnz));
+    c.scratch64.ensure(64);
+    int* wide = reinterpret_cast<int*>(c.scratch64.p + 44);
+    LF_CUDA(cudaMemsetAsync(wide, 0, sizeof(int), c.stream));
+    csr_offsets_kernel<<<grid_for(c.n, kThreads), kThreads, 0, c.stream>>>(static_cast<int>(c.n), c.rowptr, c.col,
+                                                                           c.col16, wide);
+    c.launches += 1;
     LF_CUDA(cudaGetLastError());
+    int h = 0;
+    LF_CUDA(cudaMemcpyAsync(&h, wide, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    LF_CUDA(cudaStreamSynchronize(c.stream));
+    c.col16_ok = h == 0;
     c.k32_version = c.k_version;
 }
 
