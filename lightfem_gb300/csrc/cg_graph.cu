@@ -14,10 +14,16 @@
 // CgState.  Dot products are reduced deterministically: every block publishes
 // its partial, and the last block to arrive adds them in block order.
 //
-// Products: a quarter warp per CSR row; for FP64 BSR each 2x2 block is read as
-// two 16-byte halves by a lane pair, so a warp reads 512 contiguous bytes; for
-// FP32 BSR a quarter warp reads one 16-byte block per lane.  Matrix loads carry
-// the evict-first hint so the vectors stay in L2.
+// Products: a quarter warp per CSR row or per BSR block row, several entries or
+// blocks in flight per lane (FP64 BSR: a whole 2x2 block per lane as two 16-byte
+// loads, fused multiply-adds only; FP32 BSR: one 16-byte block per lane).  The
+// FP32 products stream 16-bit column offsets from the row when they fit.  Matrix
+// loads carry the evict-first hint so the vectors stay in L2.
+//
+// The subdomain block-Jacobi preconditioner is applied by its own kernels: the
+// FP64 loop runs its block solves between the update and the r.z reduction (as
+// IC(0) runs its sweeps), the mixed loop applies FP32 block inverses after each
+// iteration's IF node.
 #include "common.cuh"
 #include "kernels.hpp"
 

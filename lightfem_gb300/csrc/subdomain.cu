@@ -9,13 +9,15 @@
 // The factor runs on the device, one CTA per subdomain, in place in the packed
 // lower factor (only the lower triangle of the dense block is ever read).  It is
 // a right-looking Cholesky: after pivot j, every entry (i, m) with j < m <= i
-// subtracts L(i, j) L(m, j).  Each entry therefore
-// subtracts its products in the same order (j ascending) as the reference's
-// row-by-row loop, and each product, difference, square root and quotient is
+// subtracts L(i, j) L(m, j).  Each entry therefore subtracts its products in the
+// same order (j ascending) as the reference's row-by-row loop, and each product, difference, square root and quotient is
 // rounded on its own.  So the factor equals the reference's bit for bit.  A block
 // whose pivot is not positive and finite becomes the identity, as there.  The
 // packed lower factor stores reciprocal pivots on its diagonal, as the
 // reference's does.
+//
+// For the mixed loop the setup also builds each block's inverse from the FP64
+// factor and stores it in FP32 as a full square (ensure_subdomain_inverse).
 #include "common.cuh"
 #include "kernels.hpp"
 #include "host_setup.hpp"
