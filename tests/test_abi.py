@@ -87,3 +87,15 @@ def test_host_subdomains_rejects_bad_arguments(native):
         assert rc == native.ERR_ARGUMENT, (per, split)
     with pytest.raises(KeyError):
         native.host_subdomains(xy, 4, "metis")
+
+
+def test_block_setting_maps_to_library_preconditioner():
+    """`preconditioner block` with subdomain_nodes 1 is the fused 2x2 nodal form;
+    any other size (the reference's default is 64) is the general subdomain form."""
+    from lightfem_gb300.model import SolverSettings
+    from lightfem_gb300.solver import gpu_preconditioner
+    assert gpu_preconditioner(SolverSettings(preconditioner="block", subdomain_nodes=1)) == "block"
+    assert gpu_preconditioner(SolverSettings(preconditioner="block")) == "subdomain"
+    assert gpu_preconditioner(SolverSettings(preconditioner="block", subdomain_nodes=7)) == "subdomain"
+    assert gpu_preconditioner(SolverSettings(preconditioner="jacobi", subdomain_nodes=7)) == "jacobi"
+    assert gpu_preconditioner(SolverSettings(preconditioner="ic0")) == "ic0"
