@@ -580,3 +580,24 @@ def test_grid6_variant_properties(native):
             assert res.solver.iterations < 0.5 * base.solver.iterations, variant
         if variant in ("bsr_block_rcb2", "bsr_block_chunk4"):
             assert res.solver.subdomains > 1 and res.solver.capture_ratio > 0.0, variant
+
+
+def test_body_and_edge_loads_equilibrium(native):
+    """tests/test_solver.cpp:233-268: a unit Q4 with a body force (0, -2) and a
+    traction (0, -3) on edge 2, clamped at nodes 1 and 4; the reactions balance
+    the applied loads, sum R_y = 5."""
+    from lightfem_gb300.model import EDGE_TRACTION, Model, SolverSettings
+    model = indexed(Model(
+        node_ids=np.array([1, 2, 3, 4]), xy=np.array([[0.0, 0.0], [1.0, 0.0], [1.0, 1.0], [0.0, 1.0]]),
+        material_ids=np.array([1]), young=np.array([1.0e6]), poisson=np.array([0.25]), thickness=np.array([1.0]),
+        element_ids=np.array([1]), element_nodes=np.array([[1, 2, 3, 4]]), element_material=np.array([1]),
+        bc_node=np.array([1, 4]), bc_ux=np.zeros(2), bc_uy=np.zeros(2),
+        body_element=np.array([1]), body_bx=np.array([0.0]), body_by=np.array([-2.0]),
+        edge_element=np.array([1]), edge_side=np.array([2]), edge_kind=np.array([EDGE_TRACTION]),
+        edge_first=np.array([0.0]), edge_second=np.array([-3.0]),
+        settings=SolverSettings(tolerance=1e-12, max_iterations=100)))
+    for precision in ("fp64", "mixed"):
+        model.settings.precision = precision
+        res = LinearElasticSolver().solve(model)
+        assert abs(res.reaction[1::2].sum() - 5.0) <= 1e-10, precision
+        assert abs(res.reaction[0::2].sum()) <= 1e-10, precision
