@@ -35,6 +35,11 @@ class ElasticProblem:
     thickness of its original material), so ``young`` has one value per element in
     element-ID order.  DOFs follow the model's node order after the optional RCM
     reordering: node ``k`` of ``node_ids`` owns DOFs ``2k`` and ``2k+1``.
+
+    ``preconditioner`` overrides the model's setting with a library name:
+    ``jacobi``, ``block`` (2x2 nodal blocks), ``subdomain`` (the model's
+    subdomain_nodes and subdomain_split) or ``ic0``.  Without it the model's
+    settings decide, as LinearElasticSolver does.
     """
 
     def __init__(self, model: Model, *, precision: str | None = None, storage: str | None = None,
