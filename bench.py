@@ -375,7 +375,7 @@ def run_ours(args) -> int:
         # --profile-iters iterations, the same loop with its kernels launched on the
         # stream, then three standalone products of each kind.  IC(0) and the
         # subdomain blocks run in FP64.
-        precision = "fp64" if args.precond in ("ic0", "subdomain") else "mixed"
+        precision = args.profile_precision or ("fp64" if args.precond in ("ic0", "subdomain") else "mixed")
         if args.precond == "subdomain":
             ctx.set_subdomains(args.subdomain_nodes, args.subdomain_split)
         capped = ctx.options(tol, args.profile_iters, args.storage, args.precond, precision, "reliable")
@@ -564,6 +564,8 @@ def main() -> int:
     ap.add_argument("--precond", choices=("jacobi", "block", "ic0", "subdomain"), default="jacobi",
                     help="block: 2x2 nodal blocks; ic0 and subdomain only with --profile-iters (FP64 profiling run)")
     ap.add_argument("--subdomain-nodes", type=int, default=64, help="nodes per subdomain for --precond subdomain")
+    ap.add_argument("--profile-precision", choices=("fp64", "mixed"), default=None,
+                    help="precision of the --profile-iters run (default: fp64 for ic0 and subdomain, else mixed)")
     ap.add_argument("--subdomain-split", choices=("rcb", "chunk"), default="rcb")
     ap.add_argument("--scale", type=int, default=1, help="divide the mesh size (testing only)")
     ap.add_argument("--fp64-steps", type=int, default=3)
