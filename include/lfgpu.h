@@ -154,6 +154,14 @@ int lfgpu_create(int device, lfgpu_t* out);
 int lfgpu_destroy(lfgpu_t h);
 const char* lfgpu_last_error(lfgpu_t h);
 const char* lfgpu_version(void);
+/* The last failure a kernel of this handle reported, for hosts that rebuild the
+ * reference's message from their own model: *status its lfgpu_status (0: none so
+ * far), *index the element index (LFGPU_ERR_JACOBIAN, LFGPU_ERR_EDGE), DOF
+ * (LFGPU_ERR_MECHANISM) or CTA (LFGPU_ERR_TIMEOUT) it names.  For
+ * LFGPU_ERR_MECHANISM values[0] and values[1] receive the DOF's constrained load
+ * and diagonal, the two numbers the zero-pivot exception prints
+ * (src/solver.cpp:926-936); otherwise both are 0.  Any pointer may be NULL. */
+int lfgpu_failure_detail(lfgpu_t h, int32_t* status, int64_t* index, double* values);
 
 /* --- model -------------------------------------------------------------------- */
 /* Nodes in index order (node k owns DOFs 2k, 2k+1: Model::rebuild_indices,

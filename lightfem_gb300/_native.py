@@ -78,6 +78,7 @@ _SIGNATURES = {
     "lfgpu_destroy": (c_int, [c_void_p]),
     "lfgpu_last_error": (c_char_p, [c_void_p]),
     "lfgpu_version": (c_char_p, []),
+    "lfgpu_failure_detail": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_int64), c_void_p]),
     "lfgpu_set_mesh": (c_int, [c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_void_p, c_int64, c_void_p,
                                c_void_p, c_void_p, c_int32]),
     "lfgpu_set_young": (c_int, [c_void_p, c_void_p]),
@@ -313,6 +314,16 @@ class Context:
         out = np.empty(size)
         self._check(self._lib.lfgpu_download(self._h, which, _ptr(out)))
         return out
+
+    def failure_detail(self) -> tuple[int, int, float, float]:
+        """(status, index, load, diagonal) of the last failure a kernel reported
+        (``lfgpu_failure_detail``); load and diagonal are set for a zero pivot
+        carrying load."""
+        status, index = c_int32(0), c_int64(0)
+        values = np.zeros(2)
+        self._check(self._lib.lfgpu_failure_detail(self._h, ctypes.byref(status), ctypes.byref(index),
+                                                   values.ctypes.data))
+        return int(status.value), int(index.value), float(values[0]), float(values[1])
 
     def timings(self) -> dict:
         t = Timings()

@@ -25,6 +25,18 @@ void check_status(Context& c) {
     DeviceStatus s{};
     LF_CUDA(cudaMemcpy(&s, c.status.p, sizeof(s), cudaMemcpyDeviceToHost));
     if (s.code == 0) return;
+    c.fail_code = s.code;
+    c.fail_index = s.bad_index;
+    c.fail_values[0] = c.fail_values[1] = 0.0;
+    if (s.code == LFGPU_ERR_MECHANISM && s.bad_index >= 0 && s.bad_index < c.n) {
+        // The sweep leaves a loaded zero pivot untouched: read its load and diagonal
+        // for the reference's message (src/solver.cpp:926-936).
+        int pos = 0;
+        LF_CUDA(cudaMemcpy(&pos, c.diag.p + s.bad_index, sizeof(int), cudaMemcpyDeviceToHost));
+        LF_CUDA(cudaMemcpy(&c.fail_values[0], c.f.p + s.bad_index, sizeof(double), cudaMemcpyDeviceToHost));
+        if (pos >= 0 && pos < c.nnz)
+            LF_CUDA(cudaMemcpy(&c.fail_values[1], c.K.p + pos, sizeof(double), cudaMemcpyDeviceToHost));
+    }
     std::string msg;
     switch (s.code) {
         case LFGPU_ERR_JACOBIAN:
@@ -295,6 +307,17 @@ int lfgpu_destroy(lfgpu_t h) {
 }
 
 const char* lfgpu_last_error(lfgpu_t h) { return h ? h->error.c_str() : "null handle"; }
+
+int lfgpu_failure_detail(lfgpu_t h, int32_t* status, int64_t* index, double* values) {
+    if (h == nullptr) return LFGPU_ERR_ARGUMENT;
+    if (status) *status = h->fail_code;
+    if (index) *index = h->fail_index;
+    if (values) {
+        values[0] = h->fail_values[0];
+        values[1] = h->fail_values[1];
+    }
+    return LFGPU_OK;
+}
 
 int lfgpu_set_mesh(lfgpu_t h, int64_t n_nodes, const double* xy, int64_t n_elements, const int32_t* element_nodes,
                    const int32_t* element_material, int64_t n_materials, const double* young, const double* poisson,

@@ -93,6 +93,12 @@ struct Context {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
     std::string error;
+    // The last failure a kernel reported (lfgpu_failure_detail): its status, the
+    // index it names and, for a zero pivot carrying load, that DOF's load and
+    // diagonal as the sweep left them.
+    int fail_code = 0;
+    i64 fail_index = -1;
+    double fail_values[2] = {0.0, 0.0};
 
     // mesh
     i64 n_nodes = 0, n_elem = 0, n_mat = 0;

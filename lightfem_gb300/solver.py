@@ -20,6 +20,7 @@ VTK/CSV output stays with the reference host library.
 
 from __future__ import annotations
 
+import math
 import time
 from dataclasses import dataclass, field
 
@@ -115,10 +116,32 @@ class AnalysisResult:
 
 
 _MESSAGES = {
+    _native.ERR_NONFINITE_DIAG: "Jacobi preconditioner encountered a non-finite diagonal",
     _native.ERR_NOT_SPD: "PCG encountered non-positive curvature; system is not SPD",
     _native.ERR_RHO_INITIAL: "PCG failed to form a positive initial preconditioned residual",
     _native.ERR_RHO: "PCG preconditioned residual became non-positive or non-finite",
 }
+
+
+def c_fixed(x: float) -> str:
+    """``std::to_string(double)``: printf's ``%f``, with C's spelling of NaN and
+    infinity."""
+    if math.isnan(x):
+        return "-nan" if math.copysign(1.0, x) < 0 else "nan"
+    if math.isinf(x):
+        return "-inf" if x < 0 else "inf"
+    return f"{x:f}"
+
+
+def mechanism_message(ctx: _native.Context, model: Model) -> str:
+    """The zero-pivot exception of src/solver.cpp:926-936, from the DOF, load and
+    diagonal the library reports and the node's ID and coordinates."""
+    _, dof, load, diag = ctx.failure_detail()
+    node = dof // 2
+    return ("the structure is a mechanism: a bar end has no transverse stiffness but carries a transverse load; "
+            f"add a support there or load the bar along its axis [dof {dof} load {c_fixed(load)} diag "
+            f"{c_fixed(diag)} node {int(model.node_ids[node])} xy {c_fixed(float(model.xy[node, 0]))},"
+            f"{c_fixed(float(model.xy[node, 1]))}]")
 
 
 def gpu_preconditioner(settings) -> str:
@@ -190,7 +213,12 @@ class LinearElasticSolver:
             perf.before = perf.after
         strategy = "atomic" if s.assembly == "atomic" or s.gpu_assembly == "atomic" else "coloring"
         ctx.assemble(strategy)
-        ctx.apply_dirichlet()
+        try:
+            ctx.apply_dirichlet()
+        except _native.GpuError as err:
+            if err.code == _native.ERR_MECHANISM:
+                raise RuntimeError(mechanism_message(ctx, model)) from err
+            raise
         if gpu_preconditioner(s) == "subdomain":
             ctx.set_subdomains(s.subdomain_nodes, s.subdomain_split)
         try:

@@ -22,16 +22,22 @@ pytestmark = pytest.mark.gpu
 _PCG_KINDS = ("rho_initial", "not_spd", "rho")
 
 
-def gpu_outcome(model, precision="fp64"):
+def gpu_outcome(model, precision="fp64", ref_message=None):
     """How LinearElasticSolver.solve ends: "converged" (with the result) or the
-    kind of the reference exception its message carries."""
+    kind of the reference exception its message carries.  An exception of the
+    reference's kind must carry ``ref_message``, the reference's own, character
+    for character (the zero-pivot one prints the DOF, its load and diagonal and
+    the node)."""
     model.settings.precision = precision
     try:
         return "converged", LinearElasticSolver().solve(model)
     except RuntimeError as err:
         if str(err).startswith("PCG did not converge"):
             return "maxit", None
-        return outcome_kind(str(err)), None
+        kind = outcome_kind(str(err))
+        if ref_message is not None and ref_message != "converged" and kind == outcome_kind(ref_message):
+            assert str(err) == ref_message
+        return kind, None
 
 
 @pytest.mark.parametrize("storage", ["csr", "bsr"])
@@ -41,7 +47,7 @@ def test_fp64_failure_matches_reference(native, golden_json, name, precond, stor
     ref = golden_json["failures"][name][f"{storage}_{precond}"]
     want = outcome_kind(ref["outcome"])
     model = failure_case(name, storage, precond)
-    got, res = gpu_outcome(model)
+    got, res = gpu_outcome(model, ref_message=ref["outcome"])
     assert got == want
     if want != "converged":
         return
@@ -59,9 +65,10 @@ def test_mixed_failure_matches_reference(native, golden_json, name, precond, sto
     fixed at the start.  On an indefinite K (negative modulus) where breakdown comes
     later, it must either break down with one of pcg_solve's errors or reach the
     FP64 target on the true residual."""
-    want = outcome_kind(golden_json["failures"][name][f"{storage}_{precond}"]["outcome"])
+    ref = golden_json["failures"][name][f"{storage}_{precond}"]
+    want = outcome_kind(ref["outcome"])
     model = failure_case(name, storage, precond)
-    got, res = gpu_outcome(model, precision="mixed")
+    got, res = gpu_outcome(model, precision="mixed", ref_message=ref["outcome"])
     if name in FAILURE_DETERMINISTIC or want == "converged":
         assert got == want
     else:
