@@ -304,13 +304,29 @@ __device__ __forceinline__ void bsr64_rows(const CgArgs& a, const G& g, Out&& ou
 
 // FP32 BSR block rows, quarter warp per block row (one 16-byte block per lane).
 // Each lane keeps three blocks in flight (k, k+4, k+8), so the nine blocks of an
-// interior node's row cost one round of gather latency instead of three.
+// interior node's row cost one round of gather latency instead of three.  The
+// grid-stride loop loads the next row's block offsets while this row's blocks
+// stream, which takes one dependent load off each row's chain.
 template <typename G, typename Out>
 __device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& out) {
-    rows_by_quad(a.nb, [&](bool act, int node, int sub) {
+    const int lane = threadIdx.x & 31, sub = lane & 3;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int stride = ((gridDim.x * blockDim.x) >> 5) * 8;
+    int node = warp * 8 + (lane >> 2);
+    int nb_b = 0, nb_e = 0;
+    if (node < a.nb) {
+        nb_b = __ldg(a.brow + node);
+        nb_e = __ldg(a.brow + node + 1);
+    }
+    for (int base = warp * 8; base < a.nb; base += stride, node += stride) {  // warp-uniform
+        const bool act = node < a.nb;
+        const int b = nb_b, e = nb_e;
+        if (node + stride < a.nb) {
+            nb_b = __ldg(a.brow + node + stride);
+            nb_e = __ldg(a.brow + node + stride + 1);
+        }
         float s0 = 0.f, s1 = 0.f;
         if (act) {
-            const int b = __ldg(a.brow + node), e = __ldg(a.brow + node + 1);
             // Columns as 16-bit offsets from the block row when they fit (half the bytes).
             auto col = [&](int k) { return a.bcol16 ? node + ld_stream(a.bcol16 + k) : ld_stream(a.bcol + k); };
             for (int k = b + sub; k < e; k += 12) {
@@ -334,7 +350,7 @@ __device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& ou
         s0 = quad_sum(s0);
         s1 = quad_sum(s1);
         if (act && sub == 0) out(node, make_float2(s0, s1));
-    });
+    }
 }
 
 // FP32 CSR rows, quarter warp per row; five entries in flight per lane cover the
