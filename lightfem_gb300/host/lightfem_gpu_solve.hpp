@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <numeric>
@@ -226,19 +227,24 @@ void check_stage(const Handle& h, const ModelT& model, int rc) {
     double values[2] = {0.0, 0.0};
     h.check(lfgpu_failure_detail(h.get(), &status, &index, values));
     if (rc == LFGPU_ERR_EDGE) {
-        bool pressure = false;
-        if (index >= 0 && static_cast<std::size_t>(index) < model.elements.size()) {
-            const int id = model.elements[static_cast<std::size_t>(index)].id;
-            for (const auto& l : model.edge_loads) {
-                using Type = decltype(l.type);
-                if (l.element_id == id) {
-                    pressure = l.type == Type::Pressure;
-                    break;
-                }
-            }
+        // The reference stops at the first zero-length loaded edge in record
+        // order; its kind names the message.
+        const auto node = index_by_id(model.nodes);
+        const auto element = index_by_id(model.elements);
+        for (const auto& l : model.edge_loads) {
+            using Type = decltype(l.type);
+            if (l.edge < 1 || l.edge > 4) continue;
+            const auto& el = model.elements[static_cast<std::size_t>(
+                find(element, l.element_id, "validated edge load references an unknown element"))];
+            const auto& a = model.nodes[static_cast<std::size_t>(
+                find(node, el.node_ids[l.edge - 1], "validated Q4 element references an unknown node"))];
+            const auto& b = model.nodes[static_cast<std::size_t>(
+                find(node, el.node_ids[l.edge % 4], "validated Q4 element references an unknown node"))];
+            if (!(std::hypot(b.position.x - a.position.x, b.position.y - a.position.y) > 1.0e-14))
+                throw std::runtime_error(l.type == Type::Pressure ? "Q4 edge pressure received a zero-length edge"
+                                                                  : "Q4 edge traction received a zero-length edge");
         }
-        throw std::runtime_error(pressure ? "Q4 edge pressure received a zero-length edge"
-                                          : "Q4 edge traction received a zero-length edge");
+        h.check(rc);
     }
     if (index < 0 || static_cast<std::size_t>(index / 2) >= model.nodes.size()) h.check(rc);
     const auto& nd = model.nodes[static_cast<std::size_t>(index / 2)];

@@ -27,7 +27,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _native
-from .model import Model
+from .model import EDGE_PRESSURE, Model
 
 
 @dataclass
@@ -144,6 +144,25 @@ def mechanism_message(ctx: _native.Context, model: Model) -> str:
             f"{c_fixed(float(model.xy[node, 1]))}]")
 
 
+def edge_message(model: Model) -> str | None:
+    """q4_edge_traction / q4_edge_pressure's exception (src/element.cpp:189, :206)
+    for the first loaded edge of zero length in record order, as the reference
+    meets them; None if the host finds none."""
+    if not model.edge_element.size:
+        return None
+    nodes = model.element_node_index()
+    elems = model.element_index(model.edge_element)
+    for k in range(elems.shape[0]):
+        side = int(model.edge_side[k])
+        if not 1 <= side <= 4:
+            continue
+        a, b = model.xy[nodes[elems[k], side - 1]], model.xy[nodes[elems[k], side % 4]]
+        if not math.hypot(b[0] - a[0], b[1] - a[1]) > 1.0e-14:
+            kind = "pressure" if int(model.edge_kind[k]) == EDGE_PRESSURE else "traction"
+            return f"Q4 edge {kind} received a zero-length edge"
+    return None
+
+
 def gpu_preconditioner(settings) -> str:
     """The library preconditioner for a reference setting: ``block`` with
     ``subdomain_nodes 1`` is the 2x2 nodal form fused into the loop kernels; any
@@ -212,7 +231,14 @@ class LinearElasticSolver:
         if s.reordering != "rcm":  # as the reference: "before" mirrors "after" without reordering
             perf.before = perf.after
         strategy = "atomic" if s.assembly == "atomic" or s.gpu_assembly == "atomic" else "coloring"
-        ctx.assemble(strategy)
+        try:
+            ctx.assemble(strategy)
+        except _native.GpuError as err:
+            if err.code == _native.ERR_JACOBIAN:
+                raise RuntimeError("Q4 stiffness evaluation received a non-positive Jacobian") from err
+            if err.code == _native.ERR_EDGE:
+                raise RuntimeError(edge_message(model) or str(err)) from err
+            raise
         try:
             ctx.apply_dirichlet()
         except _native.GpuError as err:

@@ -104,6 +104,49 @@ def floating_node(model, loaded):
     return model
 
 
+def flipped_element(model, element):
+    """``model`` with one element's nodes in clockwise order: detJ < 0 at every
+    Gauss point (q4_kinematics, src/element.cpp:52-54)."""
+    model.element_nodes[element] = model.element_nodes[element][::-1].copy()
+    return model
+
+
+def collapsed_edge(kinds):
+    """One Q4 whose nodes 3 and 4 coincide (a triangle: detJ = (1 - eta)/8 > 0 at
+    the Gauss points, so the stiffness is fine) with one edge load per entry of
+    ``kinds`` ((side, EDGE_*) pairs, in record order).  Edge 3 has zero length."""
+    from lightfem_gb300.model import EDGE_PRESSURE
+    sides = np.array([k[0] for k in kinds])
+    kind = np.array([k[1] for k in kinds])
+    return Model(
+        node_ids=np.array([1, 2, 3, 4]), xy=np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [0.0, 1.0]]),
+        material_ids=np.array([1]), young=np.array([1.0e6]), poisson=np.array([0.25]), thickness=np.array([1.0]),
+        element_ids=np.array([1]), element_nodes=np.array([[1, 2, 3, 4]]), element_material=np.array([1]),
+        bc_node=np.array([1, 2]), bc_ux=np.zeros(2), bc_uy=np.zeros(2),
+        edge_element=np.ones(len(kinds), np.int64), edge_side=sides, edge_kind=kind,
+        edge_first=np.where(kind == EDGE_PRESSURE, 1.0, 0.0), edge_second=np.where(kind == EDGE_PRESSURE, 0.0, -1.0),
+        settings=SolverSettings(tolerance=1e-12, max_iterations=100))
+
+
+# Models whose assembly stops with the reference's element exceptions
+# (src/element.cpp:52-54, :189, :206).  The "failures" entry of golden.json holds
+# how the reference ended on each.
+ASSEMBLY_FAILURES = {
+    "flipped_element": lambda: flipped_element(grid6(), 7),
+    "collapsed_edge_pressure": lambda: collapsed_edge([(1, 0), (3, 1)]),
+    "collapsed_edge_traction": lambda: collapsed_edge([(1, 1), (3, 0), (3, 1)]),
+}
+
+
+def assembly_failure_message(golden_json, name):
+    """The message the reference ended with on ASSEMBLY_FAILURES[name].  Its
+    element stiffness runs inside an OpenMP parallel region, which an exception
+    cannot leave, so a non-positive Jacobian ends the reference's process through
+    std::terminate; the golden then keeps the exception's what()."""
+    ref = golden_json["failures"][name]["csr_jacobi"]
+    return ref["what"] if ref["outcome"] == "terminate" else ref["outcome"]
+
+
 def with_load(value):
     def make():
         m = grid6()

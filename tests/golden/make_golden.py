@@ -19,7 +19,8 @@ Cases:
   strain     16x8 plane-strain cantilever with RCM (the 1000x1000 workload's physics)
   adjoint    20x20 cantilever with log-normal per-element moduli + reference FD
   failures   degenerate inputs (NaN/inf/negative moduli, NaN/inf loads, a floating
-             node): how the public solve() ends for each preconditioner and storage
+             node): how the public solve() ends for each preconditioner and storage;
+             a clockwise element and zero-length loaded edges: how the assembly ends
   cfg1       the 200x200 workload: iteration counts, residuals, sampled u and R
   cfg2       the 1000x1000 workload: known answers from the reference.  These runs
              take hours; `--run-cfg2 DIR` makes them (ref_dump output per variant
@@ -118,12 +119,15 @@ CFG2_VARIANTS = {
 
 def failure_outcomes() -> tuple[dict, dict]:
     """How the reference's public solve() ends on each model of FAILURE_MODELS
-    (tests/cases.py), for every preconditioner and storage.  Non-finite moduli and
+    (tests/cases.py), for every preconditioner and storage, and on each model of
+    ASSEMBLY_FAILURES.  Non-finite moduli and
     loads cannot pass the parser, so they go in as ref_dump overrides after
     parsing, with validation off (the solver needs only an indexed model)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from cases import FAILURE_MODELS
+    from cases import ASSEMBLY_FAILURES, FAILURE_MODELS
     outcomes, arrays = {}, {}
+    for name, make in ASSEMBLY_FAILURES.items():  # the assembly stops before any solver choice
+        outcomes[name] = {"csr_jacobi": terminating_outcome(make())}
     for name, make in FAILURE_MODELS.items():
         model = make()
         overrides = []
@@ -142,6 +146,26 @@ def failure_outcomes() -> tuple[dict, dict]:
                 if "u" in va:
                     arrays[f"{name}__{storage}_{precond}"] = va["u"]
     return outcomes, arrays
+
+
+def terminating_outcome(model: Model) -> dict:
+    """ref_dump's outcome stage on ``model``.  The reference computes element
+    stiffness inside an OpenMP parallel region, and an exception cannot leave
+    one: a non-positive Jacobian ends the process through std::terminate, which
+    prints the exception's what().  That run is recorded as
+    {"outcome": "terminate", "what": <message>}."""
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "m.fem")
+        with open(path, "w") as fh:
+            fh.write(mesh.to_fem(model, os.path.join(tmp, "out.vtk")))
+        proc = subprocess.run([REF_DUMP, path, tmp, "outcome=1", "validate=0"], capture_output=True, text=True)
+        if proc.returncode == 0:
+            with open(os.path.join(tmp, "report.json")) as fh:
+                return json.load(fh)
+    what = [line.split("what():", 1)[1].strip() for line in proc.stderr.splitlines() if "what():" in line]
+    if proc.returncode >= 0 or not what:
+        raise RuntimeError(f"ref_dump failed: {proc.stderr}")
+    return {"outcome": "terminate", "what": what[0]}
 
 
 def save(name: str, arrays: dict) -> None:

@@ -13,7 +13,8 @@ host reads after the launch: none of these cases faults, traps or hangs the GPU.
 import numpy as np
 import pytest
 
-from cases import FAILURE_DETERMINISTIC, FAILURE_MODELS, by_id_order, failure_case, outcome_kind
+from cases import ASSEMBLY_FAILURES, FAILURE_DETERMINISTIC, FAILURE_MODELS, assembly_failure_message, by_id_order, \
+    failure_case, indexed, outcome_kind
 from conftest import load_golden
 from lightfem_gb300.solver import LinearElasticSolver
 
@@ -76,3 +77,14 @@ def test_mixed_failure_matches_reference(native, golden_json, name, precond, sto
     if got == "converged" and np.all(np.isfinite(model.load_fy)):
         target = model.settings.tolerance * max(1.0, res.solver.initial_residual)
         assert res.solver.true_residual <= 1.2 * target
+
+
+@pytest.mark.parametrize("name", list(ASSEMBLY_FAILURES))
+def test_assembly_failure_message(native, golden_json, name):
+    """A clockwise element and a zero-length loaded edge stop the assembly with
+    the reference's exception text; for edges, the kind of the first failing
+    record in record order names it.  (Where the reference's OpenMP region turns
+    the Jacobian exception into std::terminate, the GPU path raises it.)"""
+    with pytest.raises(RuntimeError) as err:
+        LinearElasticSolver().solve(indexed(ASSEMBLY_FAILURES[name]()))
+    assert str(err.value) == assembly_failure_message(golden_json, name)

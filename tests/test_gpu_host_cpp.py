@@ -7,7 +7,7 @@ the reference's exception kind and message."""
 import numpy as np
 import pytest
 
-from cases import CASES, FAILURE_MODELS, VARIANTS, indexed
+from cases import ASSEMBLY_FAILURES, CASES, FAILURE_MODELS, VARIANTS, assembly_failure_message, indexed
 from conftest import load_golden
 from host_cpp import compile_driver, id_order, run
 from lightfem_gb300.solver import LinearElasticSolver
@@ -84,3 +84,9 @@ def test_failure_ends_as_the_reference(driver, golden_json, name, tmp_path):
         assert abs(int(out["report"]["iterations"]) - ref["iterations"]) <= 2
     else:
         assert (kind, message) == ("runtime_error", ref["outcome"])
+
+
+@pytest.mark.parametrize("name", list(ASSEMBLY_FAILURES))
+def test_assembly_failure_message(driver, golden_json, name, tmp_path):
+    kind, message, _ = run(driver, ASSEMBLY_FAILURES[name](), str(tmp_path))
+    assert (kind, message) == ("runtime_error", assembly_failure_message(golden_json, name))

@@ -7,7 +7,7 @@ applications are compared at rounding level.  CPU only."""
 import numpy as np
 import pytest
 
-from cases import (CASES, FAILURE_MODELS, VARIANTS, adjoint_model, by_id_order, failure_case, indexed,
+from cases import (ASSEMBLY_FAILURES, CASES, FAILURE_MODELS, assembly_failure_message, VARIANTS, adjoint_model, by_id_order, failure_case, indexed,
                    oracle_outcome, outcome_kind)
 from conftest import load_golden
 from lightfem_gb300 import mesh
@@ -211,3 +211,14 @@ def test_failure_outcomes_match_reference(oracle, golden_json, name):
         if kind == "converged":
             assert out["report"]["iterations"] == ref["iterations"], variant
             np.testing.assert_array_equal(by_id_order(model, out["u"]), g[f"{name}__{variant}"])
+
+
+@pytest.mark.parametrize("name", list(ASSEMBLY_FAILURES))
+def test_assembly_failures_stop_the_oracle(oracle, golden_json, name):
+    """A clockwise element stops the oracle's assembly with the reference's
+    Jacobian message (the reference's OpenMP build ends in std::terminate with
+    it); a zero-length loaded edge stops it too."""
+    with pytest.raises(RuntimeError) as err:
+        oracle.solve_model(indexed(ASSEMBLY_FAILURES[name]()))
+    if name == "flipped_element":
+        assert str(err.value) == assembly_failure_message(golden_json, name)
