@@ -162,9 +162,17 @@ public:
     void index_with_node_order(const std::vector<int>& node_order) {
         if (node_order.size() != nodes.size())
             throw std::invalid_argument("node reordering must contain every model node exactly once");
+        sort_by_id(materials);
+        sort_by_id(elements);
+        sort_by_id(trusses);
+        require_unique_ids(materials, "material");
+        require_unique_ids(elements, "element");
+        require_unique_ids(trusses, "truss");
         std::unordered_map<int, std::size_t> where;
         where.reserve(nodes.size());
-        for (std::size_t i = 0; i < nodes.size(); ++i) where.emplace(nodes[i].id, i);
+        for (std::size_t i = 0; i < nodes.size(); ++i)
+            if (!where.emplace(nodes[i].id, i).second)
+                throw std::logic_error("duplicate node ID: " + std::to_string(nodes[i].id));
         std::vector<Node> reordered;
         reordered.reserve(nodes.size());
         for (const int id : node_order) {
