@@ -269,15 +269,16 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* opt
  * int32[n_rows + 1], columns int32[nnz], values double[nnz], u and f double[n_rows];
  * device pointers, current device), the residual lfgpu_solve reports as
  * true_residual.  It allocates nothing: for callers that cannot allocate device
- * memory (work recorded into a CUDA graph capture, frameworks whose pool owns all
- * device memory, loops where an allocation's implicit synchronisation is not
- * acceptable).  Its only scratch is a fixed 512 KiB static device array, so
- * n_rows <= LFGPU_NOALLOC_MAX_ROWS; larger systems return LFGPU_ERR_SCRATCH_LIMIT.
- * The first call on a device resolves the array's address with that device
- * current (it may load the module there): make it before any stream capture.
- * All calls on a device share the array, which keeps the last call's contents;
- * calls that overlap on the GPU (two streams or two threads) race on it.  Runs on
- * `stream` (NULL: the legacy default stream) and synchronises it. */
+ * memory (frameworks whose pool owns all device memory, loops where an
+ * allocation's implicit synchronisation is not acceptable).  Its only scratch is
+ * a fixed 512 KiB static device array, so n_rows <= LFGPU_NOALLOC_MAX_ROWS;
+ * larger systems return LFGPU_ERR_SCRATCH_LIMIT.  The first call on a device (and
+ * the first in each new context on it) resolves the array's address with that
+ * device current, which may load the module there: make it before any stream
+ * capture.  All calls in a context share the array, which keeps the last call's
+ * contents; calls that overlap on the GPU (two streams or two threads) race on
+ * it.  Runs on `stream` (NULL: the legacy default stream), copies the norm to
+ * *norm_out and synchronises `stream` before it returns. */
 #define LFGPU_NOALLOC_MAX_ROWS 4194304
 int lfgpu_residual_norm_noalloc(int64_t n_rows, const int32_t* row_offsets, const int32_t* columns,
                                 const double* values, const double* u, const double* f, void* stream,

@@ -8,7 +8,9 @@ Output: lightfem_gb300/_lib/liblfgpu.so (git-ignored; rebuilt on every machine).
 
 from __future__ import annotations
 
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -32,18 +34,36 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblfgpu")
 
 
-def _sources_newer(target: str) -> bool:
-    if not os.path.exists(target):
-        return True
-    t = os.path.getmtime(target)
-    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "lfgpu.h"),
-                                                                  os.path.abspath(__file__)]
-    return any(os.path.getmtime(f) > t for f in files if os.path.isfile(f))
+STAMP = LIB + ".stamp"
+
+
+def _fingerprint() -> str:
+    """Hash of every source, this script, the machine type and the compiler: a
+    library built elsewhere (another architecture, other sources) never matches."""
+    h = hashlib.sha256()
+    files = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)) + [os.path.join(ROOT, "include", "lfgpu.h"),
+                                                                        os.path.abspath(__file__)]
+    for f in files:
+        if os.path.isfile(f):
+            h.update(os.path.basename(f).encode())
+            with open(f, "rb") as fh:
+                h.update(fh.read())
+    h.update(platform.machine().encode())
+    h.update(nvcc().encode())
+    return h.hexdigest()
+
+
+def _up_to_date() -> bool:
+    if not (os.path.exists(LIB) and os.path.exists(STAMP)):
+        return False
+    with open(STAMP) as fh:
+        return fh.read().strip() == _fingerprint()
 
 
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
-    """Compile liblfgpu.so if any source is newer than it; return its path."""
-    if not force and not ptxas_info and not _sources_newer(LIB):
+    """Compile liblfgpu.so unless a library built here from the same sources exists;
+    return its path."""
+    if not force and not ptxas_info and _up_to_date():
         return LIB
     os.makedirs(os.path.join(OUT_DIR, "obj"), exist_ok=True)
     nv = nvcc()
@@ -78,6 +98,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     if r.returncode != 0:
         raise RuntimeError("liblfgpu link failed:\n" + r.stdout)
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as fh:
+        fh.write(_fingerprint() + "\n")
     return LIB
 
 

@@ -1,26 +1,28 @@
 // lfgpu_residual_norm_noalloc: ||f - K u||_2 of a CSR system in caller-owned
 // device memory, computed without allocating anything.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is being
-// captured (an allocation would break the capture), code inside a host framework
-// that owns all device memory through its own pool and forbids driver
-// allocations, and latency-critical loops where an allocation (which can
-// synchronise the device) is not acceptable.  This entry point serves them: it
-// takes device pointers to the caller's arrays and keeps its only scratch -- one
-// partial sum per thread block, an arrival counter and the result -- in a
-// file-scope static device array of fixed size, allocated once when the library's
-// module is loaded on a device and held until the process exits.
+// Some callers cannot call cudaMalloc: code inside a host framework that owns all
+// device memory through its own pool and forbids driver allocations, and
+// latency-critical loops where an allocation (which can synchronise the device)
+// is not acceptable.  This entry point serves them: it takes device pointers to
+// the caller's arrays and keeps its only scratch -- one partial sum per thread
+// block, an arrival counter and the result -- in a file-scope static device array
+// of fixed size, allocated once when the library's module is loaded in a context
+// and held until the process exits.  The call copies the result to host memory
+// and synchronises the caller's stream before it returns.
 //
 // The same residual is what lfgpu_solve reports as true_residual (there through a
 // product into a scratch vector and a separate norm); here one kernel computes
 // each row's residual with the same per-row arithmetic and accumulates its square,
-// and the last block to finish adds the per-block partials in block order.
+// and the last block to finish adds the per-block partials in a fixed order, so
+// the result is deterministic.
 //
-// Every call on a device shares the one array, and the array keeps the last
+// Every call in a context shares the one array, and the array keeps the last
 // call's contents.  The arrival counter is cleared on the stream before each
 // launch; nothing else needs to start at zero.  Calls whose work overlaps on the
 // GPU (two streams, or two host threads) race on the array: issue them on one
 // stream, one after the other.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -31,7 +33,7 @@
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kRowsPerBlock = kThreads / 4;          // a quarter warp per row
+constexpr int kRowsPerBlock = kThreads / 4;          // 4 lanes per row
 constexpr int kMaxBlocks = 65536;                    // partial sums held in the scratch
 static_assert(static_cast<long long>(kMaxBlocks) * kRowsPerBlock == LFGPU_NOALLOC_MAX_ROWS,
               "one partial sum per block of the largest accepted system");
@@ -43,9 +45,42 @@ constexpr int kResultSlot = kMaxBlocks;
 constexpr int kCounterSlot = kMaxBlocks + 1;
 static __device__ __align__(256) double g_scratch[kMaxBlocks + 32];
 
-// Device address of g_scratch per device, resolved once with that device current.
-void* g_scratch_addr[kMaxDevices] = {};
+// Device address of g_scratch per device, resolved with that device current and
+// kept with the unique ID of the context it was resolved in.  A new context on the
+// device (after cudaDeviceReset, or a host framework's own driver context) loads
+// the module anew, possibly at another address, so its first call resolves again.
+struct ScratchAddress {
+    unsigned long long context_id = 0;
+    void* address = nullptr;
+};
+ScratchAddress g_scratch_addr[kMaxDevices];
 std::mutex g_scratch_mutex;
+
+// The driver's current-context queries, reached through the runtime so that the
+// library needs no link against the driver library.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+bool current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (get_current == nullptr || get_id == nullptr) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1{}, q2{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || f1 == nullptr)
+            return false;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q2 != cudaDriverEntryPointSuccess || f2 == nullptr)
+            return false;
+        get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;
+    return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 __global__ void __launch_bounds__(kThreads) residual_norm_kernel(int n, const int* __restrict__ rowptr,
                                                                   const int* __restrict__ col,
@@ -117,16 +152,22 @@ extern "C" int lfgpu_residual_norm_noalloc(int64_t n_rows, const int32_t* row_of
     if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) return LFGPU_ERR_CUDA;
     double* scratch = nullptr;
     {
-        // First call on this device: resolve the array's address with the device
-        // current.  This can load the module on the device, so the first call must
-        // come before any stream capture.
+        // First call on this device, or in a new context on it: resolve the array's
+        // address with the device current.  This can load the module in the
+        // context, so that first call must come before any stream capture.
         std::lock_guard<std::mutex> lock(g_scratch_mutex);
-        if (g_scratch_addr[device] == nullptr) {
+        ScratchAddress& slot = g_scratch_addr[device];
+        unsigned long long id = 0;
+        if (slot.address == nullptr || !current_context_id(&id) || id != slot.context_id) {
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || p == nullptr) return LFGPU_ERR_CUDA;
-            g_scratch_addr[device] = p;
+            // cudaGetSymbolAddress made the device's primary context current if
+            // no context was: record the context the address belongs to.
+            if (!current_context_id(&id)) return LFGPU_ERR_CUDA;
+            slot.address = p;
+            slot.context_id = id;
         }
-        scratch = static_cast<double*>(g_scratch_addr[device]);
+        scratch = static_cast<double*>(slot.address);
     }
     if (n_rows == 0) {
         *norm_out = 0.0;

@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures from the reference's own sources.
 
-Run from the repository root in a container where the reference tree is mounted:
+Run from the repository root on a machine with the reference's source tree:
 
-    make -C oracle ref          # builds oracle/_ref/ref_dump from the reference sources
+    make -C oracle ref REF=<reference checkout>   # oracle/_ref/ref_dump from its sources
     python tests/golden/make_golden.py
 
 Each case writes a small model through ``lightfem_gb300.mesh.to_fem``, runs

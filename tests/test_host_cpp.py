@@ -21,7 +21,9 @@ def test_binding_compiles_against_reference_types():
     """tests/host/reference_binding.cpp instantiates the solve template with
     lightfem::Model and lightfem::AnalysisResult (include/lightfem/model.hpp,
     include/lightfem/solver.hpp)."""
-    out = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "tests", "host"), "binding-check"],
+    from oracle.reference import make_args
+
+    out = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "tests", "host"), "binding-check", *make_args()],
                          capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     if "unavailable" in out.stdout:

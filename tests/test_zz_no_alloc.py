@@ -22,11 +22,15 @@ def test_rejects_systems_beyond_the_scratch(native):
         native.residual_norm_noalloc(native.NOALLOC_MAX_ROWS + 1, None, None, None, None, None)
 
 
+# 160x48 elements: 15,778 rows, 247 blocks of 64 rows, so the last block's final
+# sum reads each partial in one pass.  400x100: 81,002 rows, 1,266 blocks, so
+# every thread of the last block adds several partials.
 @pytest.mark.gpu
-def test_matches_solve_true_residual_on_consecutive_calls(native):
+@pytest.mark.parametrize("nx,ny", [(160, 48), (400, 100)])
+def test_matches_solve_true_residual_on_consecutive_calls(native, nx, ny):
     torch = pytest.importorskip("torch")
     assert torch.cuda.is_available()
-    model = mesh.cantilever(160, 48)
+    model = mesh.cantilever(nx, ny)
     model.sort_and_index()
     ctx = native.Context(0)
     upload_model(ctx, model)
