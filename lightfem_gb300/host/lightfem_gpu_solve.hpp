@@ -1,8 +1,34 @@
 /*
- * lightfem_gpu_solve.hpp — the staged GPU solve over liblfgpu's C ABI as a
- * template over the host's model and result types.  Include it alone to call it
- * with the reference's own types; lightfem_gpu.hpp adds mirror types for hosts
- * without them.  Header-only; link with -llfgpu.
+ * lightfem_gpu_solve.hpp — LinearElasticSolver::solve on the GPU for C++ hosts,
+ * over liblfgpu's C ABI (include/lfgpu.h).  Header-only; link with -llfgpu.
+ *
+ * lightfem_gpu::solve(model, result, device) is a template over the host's own
+ * model and result types.  It reads and writes only members that the reference's
+ * types have (Model, Node, Material, Q4Element, DirichletBC, NodalLoad,
+ * BodyForce, EdgeLoad, SolverSettings in include/lightfem/model.hpp;
+ * AnalysisResult, LinearSolverReport, PerformanceReport, ElementResult,
+ * NodeResult in include/lightfem/solver.hpp), so src/solver.cpp can hand it
+ * lightfem::Model and lightfem::AnalysisResult unchanged.  The one member it
+ * cannot fill generically is the retained CSR stiffness: the host provides
+ * assign_stiffness(CsrMatrix&, rows, row_offsets, columns, values), found by
+ * argument-dependent lookup.
+ *
+ * The stages follow LinearElasticSolver::solve (src/solver.cpp:875-960): RCM
+ * (:886-892), pattern + map + colours, element stiffness + assembly + loads
+ * (assemble, :219-334), retained K and f, Dirichlet elimination and the
+ * zero-pivot sweep (:908-940), solve_iterative (:675-747), the "PCG did not
+ * converge" check (:948-950), reactions (:953-954), postprocess and nodal
+ * smoothing (:955-957).  Failures raise the reference's exception kinds with its
+ * messages: std::invalid_argument for a bad argument, std::logic_error for a
+ * call-order error, std::runtime_error for everything the reference reports at
+ * run time.
+ *
+ * Selection follows the .fem keys: settings.solver "gpu_mixed" runs the FP32-inner
+ * PCG inside FP64 refinement, any other value FP64 PCG; settings.assembly
+ * "atomic" or "gpu_atomic" scatters with atomics, any other value by colours;
+ * preconditioner "block" with subdomain_nodes 1 is the fused 2x2 nodal form, any
+ * other subdomain_nodes the general subdomain block-Jacobi.  The GPU path
+ * assembles Q4 elements only: a model with truss bars is refused.
  */
 #pragma once
 

@@ -1,4 +1,5 @@
-// Test driver of the C++ host layer (lightfem_gb300/host/lightfem_gpu.hpp).
+// Test driver of the C++ host layer (lightfem_gb300/host/lightfem_gpu_solve.hpp),
+// over the mirror types of mirror_model.hpp.
 //
 //   solve_model <model.txt> <out_dir> [--no-index]
 //
@@ -22,7 +23,7 @@
 //   load <node> <fx> <fy>
 //   body <element> <bx> <by>
 //   edge <element> <side> <traction|pressure> <first> <second>
-#include "lightfem_gpu.hpp"
+#include "mirror_model.hpp"
 
 #include <cstdio>
 #include <cstdlib>

@@ -1,4 +1,4 @@
-"""Drive the C++ host layer (lightfem_gb300/host/lightfem_gpu.hpp) from the tests:
+"""Drive the C++ host layer (lightfem_gb300/host/lightfem_gpu_solve.hpp) from the tests:
 compile tests/host/solve_model.cpp against liblfgpu, write a model in its line
 format, run it and read back what it wrote."""
 

@@ -1,5 +1,5 @@
 """The C++ host layer on the GPU: LinearElasticSolver::solve through
-lightfem_gpu::solve (lightfem_gb300/host/lightfem_gpu.hpp) reaches the reference's
+lightfem_gpu::solve (lightfem_gb300/host/lightfem_gpu_solve.hpp) reaches the reference's
 results, gives the Python host's arrays bit for bit (both drive the same C ABI in
 the same stage order), and ends every failure model the reference's way, with
 the reference's exception kind and message."""
