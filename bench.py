@@ -65,6 +65,7 @@ class Dist:
 
     def __init__(self, world: int):
         self.world = world
+        self.rank = int(os.environ.get("RANK", "0"))
         self.dist = None
         if world > 1:
             import torch.distributed as dist
@@ -203,11 +204,13 @@ def reference_iterations(storage: str, precond: str) -> tuple[int, str]:
 
 
 def cpu_solve_sample(model, storage: str, precond: str, sample_iters: int, threads: int = 0) -> dict:
-    """Time the reference algorithm (oracle restatement) on the host: assembly,
-    elimination, preconditioner setup, `sample_iters` PCG iterations and the
-    reactions product; the PCG time is extrapolated to the reference's iteration
-    count for this model.  TEST/BASELINE INFRASTRUCTURE: this is the only place
-    bench.py runs the oracle."""
+    """Time the reference algorithm (oracle restatement, with the reference's
+    threading: colour-parallel scatter, row-parallel products, serial level-1
+    work) on the host: assembly, loads, elimination, preconditioner setup, PCG and
+    the reactions product.  ``sample_iters`` > 0 caps the PCG at that many
+    iterations and extrapolates its time to the reference's iteration count for
+    this model; 0 runs the complete solve and measures it.  TEST/BASELINE
+    INFRASTRUCTURE: this is the only place bench.py runs the oracle."""
     from oracle import lf_oracle as O
     if threads > 0:
         O.set_threads(threads)
@@ -216,6 +219,7 @@ def cpu_solve_sample(model, storage: str, precond: str, sample_iters: int, threa
     out = O.solve_model(m, stop_after="dirichlet", assembly="coloring")
     setup_total = (time.perf_counter() - t0) * 1e3
     asm_ms = out["timing"]["assembly_ms"]
+    loads_ms = out["timing"]["loads_ms"]
     bnd_ms = out["timing"]["boundary_ms"]
     t1 = time.perf_counter()
     u, rep = O.pcg(out["rowptr"], out["col"], out["Kc"], out["fc"], 1e-8, 10 ** 6, storage, precond, "chunk", 1,
@@ -228,11 +232,15 @@ def cpu_solve_sample(model, storage: str, precond: str, sample_iters: int, threa
     per_iter = rep["solve_ms"] / iters
     outside_loop = pcg_total - rep["solve_ms"]  # BSR conversion + preconditioner setup
     full_iters, key = reference_iterations(storage, precond)
-    value = asm_ms + bnd_ms + outside_loop + per_iter * full_iters + react_ms
+    if sample_iters > 0:
+        value = asm_ms + loads_ms + bnd_ms + outside_loop + per_iter * full_iters + react_ms
+    else:
+        value = asm_ms + loads_ms + bnd_ms + pcg_total + react_ms
     return {"value": value, "per_iter_ms": per_iter, "sample_iters": iters, "full_iters": full_iters,
-            "iters_source": f"reference run on this model ({key})", "assembly_ms": asm_ms, "boundary_ms": bnd_ms,
-            "pcg_setup_ms": outside_loop, "reactions_ms": react_ms, "threads": O.num_threads(),
-            "untimed_setup_ms": setup_total - asm_ms - bnd_ms}
+            "measured": sample_iters == 0, "iterations": rep["iterations"], "converged": bool(rep["converged"]),
+            "iters_source": f"reference run on this model ({key})", "assembly_ms": asm_ms, "loads_ms": loads_ms,
+            "boundary_ms": bnd_ms, "pcg_setup_ms": outside_loop, "pcg_ms": pcg_total, "reactions_ms": react_ms,
+            "threads": O.num_threads(), "untimed_setup_ms": setup_total - asm_ms - loads_ms - bnd_ms}
 
 
 def run_reference(args) -> int:
@@ -241,26 +249,43 @@ def run_reference(args) -> int:
         return 0
     model = build_model(args.scale)
     storage, precond = args.storage, args.precond if args.precond != "block" else "block"
-    values = []
-    last = None
-    for k in range(args.warmup + args.steps):
+    # Warm-up steps: bounded samples.  Timed steps: the first is the complete solve
+    # (every PCG iteration runs, nothing extrapolated) and gives the value; the
+    # others are bounded samples whose extrapolation is reported beside it, with its
+    # error against the complete solve.
+    for k in range(args.warmup):
         r = cpu_solve_sample(model, storage, precond, args.ref_sample_iters)
-        if k >= args.warmup:
-            values.append(r["value"])
-        last = r
-        log(f"reference step {k}: {r['value']:.1f} ms (per-iteration {r['per_iter_ms']:.3f} ms)")
-    value = statistics.median(values) if values else last["value"]
-    sample = (f"{last['sample_iters']} PCG iterations per step ({storage}/{precond}, FP64) plus full assembly, "
-              f"elimination, setup and reactions; loop time extrapolated to the reference's {last['full_iters']} "
-              f"iterations")
+        log(f"reference warm-up {k}: {r['value']:.1f} ms extrapolated (per-iteration {r['per_iter_ms']:.3f} ms)")
+    t_timed = time.perf_counter()
+    full = cpu_solve_sample(model, storage, precond, 0)
+    log(f"reference complete solve: {full['value']:.1f} ms, {full['iterations']} iterations")
+    samples = []
+    for k in range(1, args.steps):
+        r = cpu_solve_sample(model, storage, precond, args.ref_sample_iters)
+        samples.append(r)
+        log(f"reference step {k}: {r['value']:.1f} ms extrapolated (per-iteration {r['per_iter_ms']:.3f} ms)")
+    timed_s = time.perf_counter() - t_timed
+    value = full["value"]
+    extrapolated = statistics.median(r["value"] for r in samples) if samples else None
+    sample = (f"step 1: the complete solve ({full['iterations']} FP64 PCG iterations, {storage}/{precond}) with "
+              f"assembly, loads, elimination, setup and reactions, measured; steps 2..{args.steps}: "
+              f"{args.ref_sample_iters} PCG iterations each, loop time extrapolated to the reference's "
+              f"{full['full_iters']} iterations")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "ms", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 3), "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(timed_s * 1e3 / max(1, args.steps), 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
         "config": {"workload": WORKLOAD, "precision": "fp64", "storage": storage, "preconditioner": precond,
                    "tolerance": 1e-8, "step": STEP_DESC},
-        "cpu_baseline": {"value": round(value, 3), "unit": "ms", "cores": last["threads"], "kind": "port",
-                         "sample": sample, "per_iter_ms": round(last["per_iter_ms"], 4)},
+        "cpu_baseline": {"value": round(value, 3), "unit": "ms", "cores": full["threads"], "kind": "port",
+                         "sample": sample, "full_solve_ms": round(full["value"], 3),
+                         "full_solve_iterations": full["iterations"], "full_solve_converged": full["converged"],
+                         "full_solve_parts_ms": {k: round(full[k], 1) for k in (
+                             "assembly_ms", "loads_ms", "boundary_ms", "pcg_setup_ms", "pcg_ms", "reactions_ms")},
+                         "extrapolated_median_ms": None if extrapolated is None else round(extrapolated, 3),
+                         "extrapolation_error_pct": None if extrapolated is None else round(
+                             100.0 * (extrapolated - full["value"]) / full["value"], 2),
+                         "per_iter_ms": round(full["per_iter_ms"], 4)},
         "e2e": {"value": round(value, 3), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -285,12 +310,97 @@ def pinned(a: np.ndarray) -> np.ndarray:
         return np.ascontiguousarray(a)
 
 
+def cpu_adjoint(model, tip_dof: int, sample_iters: int = 0, iterations: tuple[int, int] | None = None) -> dict:
+    """The CPU FP64 gradient of the tip-node y displacement with respect to every
+    element modulus, on all host cores: the oracle's forward solve (assembly, loads,
+    elimination, 2x2 nodal block PCG on BSR), its adjoint solve K lambda = e_tip
+    (zeroed on constrained DOFs) and its element loop g_e = -lambda_e^T K_e u_e /
+    E_e.  The reference has no adjoint: this is the repository's restatement on the
+    reference's algorithm and threading.  ``sample_iters`` > 0 caps both PCG solves
+    and extrapolates their loop time to ``iterations`` (forward, adjoint); 0 runs
+    and measures the complete solves.  BASELINE INFRASTRUCTURE (the oracle)."""
+    from oracle import lf_oracle as O
+    m = model.copy()
+    m.settings.reordering = "none"
+    t0 = time.perf_counter()
+    out = O.solve_model(m, stop_after="dirichlet", assembly="coloring")
+    tm = out["timing"]
+    setup_ms = tm["assembly_ms"] + tm["loads_ms"] + tm["boundary_ms"]
+    parts = {"assembly_loads_dirichlet_ms": setup_ms}
+    solves = {}
+    u = None
+    for name, rhs in (("forward", out["fc"]), ("adjoint", None)):
+        if rhs is None:
+            rhs = np.zeros(m.n_dofs)
+            rhs[tip_dof] = 1.0
+            rhs[out["constraint_dofs"]] = 0.0
+        t = time.perf_counter()
+        x, rep = O.pcg(out["rowptr"], out["col"], out["Kc"], rhs, 1e-8, 10 ** 6, "bsr", "block", "chunk", 1, m.xy,
+                       iteration_cap=sample_iters)
+        total = (time.perf_counter() - t) * 1e3
+        its = max(1, rep["iterations"])
+        if sample_iters > 0 and iterations is not None:
+            full = iterations[0 if name == "forward" else 1]
+            ms = total - rep["solve_ms"] + rep["solve_ms"] / its * full
+        else:
+            full, ms = rep["iterations"], total
+        solves[name] = {"ms": round(ms, 1), "iterations": full, "measured": sample_iters == 0}
+        parts[f"{name}_solve_ms"] = ms
+        if name == "forward":
+            u = x
+        else:
+            lam = x
+    en = m.element_node_index()
+    mi = m.material_index(m.element_material)
+    t = time.perf_counter()
+    O.adjoint_grad(m.xy, en, m.young[mi], m.poisson[mi], m.thickness[mi], m.settings.plane_mode, u, lam)
+    parts["gradient_loop_ms"] = (time.perf_counter() - t) * 1e3
+    return {"ms": round(sum(parts.values()), 1), "cores": O.num_threads(), "kind": "port",
+            "parts_ms": {k: round(v, 1) for k, v in parts.items()}, "solves": solves,
+            "untimed_setup_ms": round((time.perf_counter() - t0) * 1e3 - sum(parts.values()), 1)}
+
+
+def adjoint_gpu_runs(model, tip_of, precisions, repeats: int, dist: Dist) -> tuple[dict, dict]:
+    """Forward solve + adjoint solve + gradient on the GPU (device time, CUDA
+    events), per precision: the mean over ``repeats`` runs after one warm run."""
+    from lightfem_gb300.adjoint import ElasticProblem
+    out, grads = {}, {}
+    for precision in precisions:
+        p = ElasticProblem(model, precision=precision, storage="bsr", preconditioner="block", tolerance=1e-8,
+                           max_iterations=400000)
+        y0 = p.young0.copy()
+        dj = np.zeros(p.n_dofs)
+        dj[tip_of(p)] = 1.0
+        times, kernel = [], []
+        for k in range(repeats + 1):
+            p.ctx.event_record(4)
+            p.solve(y0)
+            g = p.gradient(dj)
+            p.ctx.event_record(5)
+            if k > 0:
+                times.append(p.ctx.event_elapsed(4, 5))
+                kernel.append(p.ctx.timings()["adjoint_kernel_ms"])
+        grads[precision] = g
+        out[precision] = {"ms": round(dist.max(statistics.mean(times)), 3),
+                          "gradient_kernel_ms": round(statistics.mean(kernel), 4),
+                          "forward_iterations": p.report.iterations, "forward_refinements": p.report.refinements,
+                          "forward_fallback_fp64": int(p.report.fallback_fp64),
+                          "adjoint_iterations": p.adjoint_report.iterations,
+                          "adjoint_fallback_fp64": int(p.adjoint_report.fallback_fp64)}
+        p.close()
+    return out, grads
+
+
 def adjoint_leg(args, dist: Dist) -> dict:
     """Adjoint at scale: the perturbed two-material beam geometry at 1000x1000 with
     log-normal element moduli (2,004,002 DOFs, 1,000,000 moduli).  Timed together:
     assembly, the forward mixed-precision PCG solve, the adjoint PCG solve for the
     tip-node y displacement and the gradient kernel (device time, CUDA events).  The
-    gradient error is against an FP64 GPU forward + adjoint run on the same inputs."""
+    gradient error is against an FP64 GPU forward + adjoint run on the same inputs.
+    Also: the 400x400 log-normal cantilever (321,602 DOFs, 160,000 moduli) on the
+    GPU in both precisions, and the CPU FP64 gradient of both workloads on all host
+    cores (400x400 complete; 1000x1000 with both solves sampled and extrapolated to
+    the GPU FP64 run's iteration counts)."""
     from lightfem_gb300 import mesh
     from lightfem_gb300.adjoint import ElasticProblem
 
@@ -340,6 +450,70 @@ def adjoint_leg(args, dist: Dist) -> dict:
     ref = grads["fp64"]
     out["grad_rel_err_vs_fp64"] = float(np.linalg.norm(grads["mixed"] - ref) / np.linalg.norm(ref))
     out["speedup_mixed_vs_fp64"] = round(out["fp64"]["ms"] / out["mixed"]["ms"], 3)
+
+    # 400x400 log-normal cantilever: GPU both precisions, CPU complete.
+    m4 = mesh.workload(4, scale=args.scale)
+    m4.sort_and_index()
+    tip4 = lambda p: p.dof(mesh.tip_node_id(p.model), 1)  # noqa: E731
+    g4, gr4 = adjoint_gpu_runs(m4, tip4, ("mixed", "fp64"), 3, dist)
+    out["cfg4"] = {"workload": "400x400 plane-stress cantilever, log-normal E_e = 1 GPa exp(0.5 z), 321,602 DOFs, "
+                               "160,000 element moduli", **g4,
+                   "grad_rel_err_vs_fp64": float(np.linalg.norm(gr4["mixed"] - gr4["fp64"]) /
+                                                 np.linalg.norm(gr4["fp64"]))}
+    if dist.rank == 0 and not args.no_cpu:
+        p4 = ElasticProblem(m4, precision="fp64", storage="bsr", preconditioner="block", tolerance=1e-8)
+        tip_dof4 = tip4(p4)
+        p4.close()
+        out["cfg4"]["cpu"] = cpu_adjoint(m4, tip_dof4)
+        out["cfg4"]["speedup_gpu_mixed_vs_cpu"] = round(out["cfg4"]["cpu"]["ms"] / g4["mixed"]["ms"], 2)
+        # 1000x1000: the two CPU solves sampled, extrapolated to the GPU FP64 iteration counts.
+        p5 = ElasticProblem(model, precision="fp64", storage="bsr", preconditioner="block", tolerance=1e-8)
+        tip_dof5 = p5.dof(mesh.tip_node_id(p5.model), 1)
+        p5.close()
+        its = (out["fp64"]["forward_iterations"], out["fp64"]["adjoint_iterations"])
+        out["cpu"] = cpu_adjoint(model, tip_dof5, sample_iters=args.cpu_sample_iters, iterations=its)
+        out["cpu"]["note"] = (f"both PCG solves capped at {args.cpu_sample_iters} iterations and extrapolated to "
+                              f"the GPU FP64 run's {its[0]} + {its[1]} iterations; assembly, loads, elimination "
+                              f"and the gradient loop measured")
+        out["speedup_gpu_mixed_vs_cpu"] = round(out["cpu"]["ms"] / out["mixed"]["ms"], 2)
+    return out
+
+
+def beam_leg(args, dist: Dist) -> dict:
+    """The 2000x1000 perturbed two-material beam (4,006,002 DOFs, 72,036,004
+    nonzeros; gravity plus a 1 MPa top pressure): the same step (assembly, loads,
+    Dirichlet, PCG to 1e-8, reactions) with mixed 2x2 nodal block-Jacobi PCG (FP32
+    inner, FP64 refinement) and with FP64 PCG, BSR storage, device time."""
+    from lightfem_gb300 import _native, mesh
+    from lightfem_gb300.solver import upload_model
+
+    model = mesh.workload(3, scale=args.scale)
+    model.sort_and_index()
+    ctx = _native.Context(dist_env()[2])
+    upload_model(ctx, model)
+    out = {"workload": "2000x1000 perturbed two-material Q4 beam (4.0 m x 2.0 m, E 200/70 GPa), gravity + 1 MPa "
+                       "top pressure, 4,006,002 DOFs", "nnz": ctx.nnz, "storage": "bsr", "preconditioner": "block"}
+    for precision in ("mixed", "fp64"):
+        o = ctx.options(1e-8, 400000, "bsr", "block", precision, "reliable")
+        times = []
+        for k in range(2):
+            ctx.event_record(0)
+            ctx.assemble("coloring")
+            ctx.apply_dirichlet()
+            _, rep = ctx.solve(o, download=False)
+            ctx.reactions(download=False)
+            ctx.event_record(1)
+            if k > 0 or precision == "fp64":
+                times.append(ctx.event_elapsed(0, 1))
+            if precision == "fp64":
+                break
+        out[precision] = {"step_ms": round(dist.max(statistics.mean(times)), 2), "solve_ms": round(rep.solve_ms, 2),
+                          "iterations": rep.iterations, "refinements": rep.refinements,
+                          "true_residual_rel": rep.true_residual / rep.initial_residual,
+                          "final_residual_rel": rep.final_residual / rep.initial_residual,
+                          "fallback_fp64": int(rep.fallback_fp64)}
+    out["speedup_mixed_vs_fp64"] = round(out["fp64"]["step_ms"] / out["mixed"]["step_ms"], 3)
+    ctx.close()
     return out
 
 
@@ -434,6 +608,8 @@ def run_ours(args) -> int:
     for prec, st, pc, pers in (("mixed", "bsr", "block", False), ("mixed", "csr", "jacobi", False),
                                ("fp64", "csr", "jacobi", False), ("fp64", "bsr", "block", False),
                                ("mixed", "bsr", "subdomain", False),
+                               ("mixed", "csr", "ic0", False), ("mixed", "bsr", "ic0", False),
+                               ("fp64", "csr", "ic0", False),
                                ("mixed", "bsr", "jacobi", True), ("fp64", "csr", "jacobi", True)):
         try:
             ms, r = step(opts(prec, st, pc, pers))
@@ -441,7 +617,10 @@ def run_ours(args) -> int:
                              **({"subdomain_nodes": 64, "subdomain_split": "rcb"} if pc == "subdomain" else {}),
                              "loop": "persistent" if pers else "graph", "step_ms": round(ms, 2),
                              "solve_ms": round(r.solve_ms, 2), "iterations": r.iterations,
-                             "refinements": r.refinements, "true_residual_rel": r.true_residual / r.initial_residual})
+                             "refinements": r.refinements, "true_residual_rel": r.true_residual / r.initial_residual,
+                             "final_residual_rel": r.final_residual / r.initial_residual,
+                             **({"ic0_levels": r.ic0_levels, "setup_ms": round(r.preconditioner_setup_ms, 2)}
+                                if pc == "ic0" else {})})
         except _native.GpuError as e:
             variants.append({"precision": prec, "storage": st, "preconditioner": pc, "error": str(e)})
     ctx.assemble("coloring")
@@ -511,6 +690,7 @@ def run_ours(args) -> int:
     e2e_ms = dist.max(statistics.mean(e2e_times))
 
     adjoint = None if args.no_adjoint else adjoint_leg(args, dist)
+    beam = None if args.no_beam else beam_leg(args, dist)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -530,8 +710,10 @@ def run_ours(args) -> int:
             "solve_ms": round(rep.solve_ms, 3),
             "fp64": {"step_ms": round(fp64_ms, 3), "iterations": fp64_rep.iterations,
                      "true_residual_rel": fp64_rep.true_residual / fp64_rep.initial_residual,
+                     "final_residual_rel": fp64_rep.final_residual / fp64_rep.initial_residual,
                      "solve_ms": round(fp64_rep.solve_ms, 3)},
             "speedup_mixed_vs_fp64": round(fp64_ms / ms_step, 3),
+            "true_residual_rel_mixed_fp64": [true_rel, fp64_rep.true_residual / fp64_rep.initial_residual],
             "mixed_vs_fp64_u_rel": float(np.linalg.norm(u - u64) / np.linalg.norm(u64)),
             "reaction_sum_y": float(R[1::2].sum()),
             "postprocess_ms": round(postprocess_ms, 3),
@@ -539,6 +721,7 @@ def run_ours(args) -> int:
             "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
             "adjoint": adjoint,
+            "beam_2000x1000": beam,
             "wall_s_timed": round(wall, 3),
         }
         if cpu is not None:
@@ -576,6 +759,7 @@ def main() -> int:
     ap.add_argument("--roofline-passes", type=int, default=200,
                     help="loop passes launched on the stream to time the inner product per launch")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
+    ap.add_argument("--no-beam", action="store_true", help="skip the 2000x1000 beam measurement")
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling run for ncu: one step capped at this many PCG iterations (not a benchmark)")
     args = ap.parse_args()

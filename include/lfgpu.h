@@ -76,6 +76,17 @@ enum { LFGPU_SPLIT_RCB = 0, LFGPU_SPLIT_CHUNK = 1 };
 enum { LFGPU_PRECISION_FP64 = 0, LFGPU_PRECISION_MIXED = 1 };
 enum { LFGPU_REFINE_RELIABLE = 0, LFGPU_REFINE_RESTART = 1 };
 enum { LFGPU_EDGE_TRACTION = 0, LFGPU_EDGE_PRESSURE = 1 };
+/* Handle options (lfgpu_set_option). */
+enum {
+    LFGPU_OPTION_WAIT_LIMIT_NS = 0, /* how long a bounded device-side wait spins before it gives up with
+                                       LFGPU_ERR_TIMEOUT (default 4e9 ns); tests shorten it */
+    LFGPU_OPTION_IC0_SWEEP = 1      /* LFGPU_IC0_SWEEP_*: how the IC(0) triangular sweeps are scheduled */
+};
+/* AUTO: by levels (one thread-block cluster walks the dependency levels) when the
+ * pattern's level schedule fits the cluster's shared-memory ring, else POLLED.
+ * LEVELS: by levels, LFGPU_ERR_UNSUPPORTED where the schedule does not fit.
+ * POLLED: row chunks in sweep order, each row polling for its operands (FP64 only). */
+enum { LFGPU_IC0_SWEEP_AUTO = 0, LFGPU_IC0_SWEEP_LEVELS = 1, LFGPU_IC0_SWEEP_POLLED = 2 };
 
 /* Arrays lfgpu_download can return. */
 enum {
@@ -147,6 +158,7 @@ typedef struct lfgpu_timings {
     int64_t kernel_launches; /* kernels this handle has launched so far (graph nodes included) */
     double postprocess_ms;   /* element fields + nodal smoothing (lfgpu_postprocess) */
     double rcm_ms;           /* lfgpu_rcm (host wall time, device work included) */
+    double adjoint_kernel_ms; /* lfgpu_adjoint: the gradient kernel alone (no solve, no download) */
 } lfgpu_timings;
 
 /* --- handle ------------------------------------------------------------------- */
@@ -160,8 +172,13 @@ const char* lfgpu_version(void);
  * (LFGPU_ERR_MECHANISM) or CTA (LFGPU_ERR_TIMEOUT) it names.  For
  * LFGPU_ERR_MECHANISM values[0] and values[1] receive the DOF's constrained load
  * and diagonal, the two numbers the zero-pivot exception prints
- * (src/solver.cpp:926-936); otherwise both are 0.  Any pointer may be NULL. */
+ * (src/solver.cpp:926-936); for LFGPU_ERR_TIMEOUT values[0] is 1 when the wait
+ * raised the abort flag that stops every other wait; otherwise both are 0.  Any
+ * pointer may be NULL. */
 int lfgpu_failure_detail(lfgpu_t h, int32_t* status, int64_t* index, double* values);
+/* Set a handle option (LFGPU_OPTION_*).  No reference counterpart: the reference
+ * has no device waits and sweeps serially. */
+int lfgpu_set_option(lfgpu_t h, int32_t option, int64_t value);
 
 /* --- model -------------------------------------------------------------------- */
 /* Nodes in index order (node k owns DOFs 2k, 2k+1: Model::rebuild_indices,

@@ -29,6 +29,8 @@ SUBDOMAIN_MAX_DOFS = 1024  # LFGPU_SUBDOMAIN_MAX_DOFS
 PRECISION = {"fp64": 0, "mixed": 1}
 REFINEMENT = {"reliable": 0, "restart": 1}
 K_FULL, K_CONSTRAINED, F_FULL, F_CONSTRAINED, U, R = range(6)
+OPTION_WAIT_LIMIT_NS, OPTION_IC0_SWEEP = 0, 1  # lfgpu_set_option
+IC0_SWEEP = {"auto": 0, "levels": 1, "polled": 2}
 
 
 class SolveOptions(ctypes.Structure):
@@ -57,7 +59,7 @@ class Report(ctypes.Structure):
 class Timings(ctypes.Structure):
     _fields_ = [("pattern_ms", c_double), ("assembly_ms", c_double), ("boundary_ms", c_double),
                 ("reactions_ms", c_double), ("coloring_count", c_int64), ("kernel_launches", c_int64),
-                ("postprocess_ms", c_double), ("rcm_ms", c_double)]
+                ("postprocess_ms", c_double), ("rcm_ms", c_double), ("adjoint_kernel_ms", c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -79,6 +81,7 @@ _SIGNATURES = {
     "lfgpu_last_error": (c_char_p, [c_void_p]),
     "lfgpu_version": (c_char_p, []),
     "lfgpu_failure_detail": (c_int, [c_void_p, POINTER(c_int32), POINTER(c_int64), c_void_p]),
+    "lfgpu_set_option": (c_int, [c_void_p, c_int32, c_int64]),
     "lfgpu_set_mesh": (c_int, [c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_void_p, c_int64, c_void_p,
                                c_void_p, c_void_p, c_int32]),
     "lfgpu_set_young": (c_int, [c_void_p, c_void_p]),
@@ -213,6 +216,10 @@ class Context:
 
     def __exit__(self, *exc):
         self.close()
+
+    def set_option(self, option: int, value: int) -> None:
+        """lfgpu_set_option: OPTION_WAIT_LIMIT_NS (ns) or OPTION_IC0_SWEEP (IC0_SWEEP values)."""
+        self._check(self._lib.lfgpu_set_option(self._h, option, value))
 
     # -- model
     def set_mesh(self, xy, element_nodes, element_material, young, poisson, thickness, plane_mode: int) -> None:

@@ -28,6 +28,7 @@ void check_status(Context& c) {
     c.fail_code = s.code;
     c.fail_index = s.bad_index;
     c.fail_values[0] = c.fail_values[1] = 0.0;
+    if (s.code == LFGPU_ERR_TIMEOUT) c.fail_values[0] = s.abort != 0u ? 1.0 : 0.0;  // the abort flag it raised
     if (s.code == LFGPU_ERR_MECHANISM && s.bad_index >= 0 && s.bad_index < c.n) {
         // The sweep leaves a loaded zero pivot untouched: read its load and diagonal
         // for the reference's message (src/solver.cpp:926-936).
@@ -65,6 +66,7 @@ void check_status(Context& c) {
 void reset_status(Context& c) {
     DeviceStatus s{};
     s.bad_index = 0x7fffffff;
+    s.wait_limit_ns = c.wait_limit_ns;
     LF_CUDA(cudaMemcpyAsync(c.status.p, &s, sizeof(s), cudaMemcpyHostToDevice, c.stream));
 }
 
@@ -319,6 +321,27 @@ int lfgpu_failure_detail(lfgpu_t h, int32_t* status, int64_t* index, double* val
     return LFGPU_OK;
 }
 
+int lfgpu_set_option(lfgpu_t h, int32_t option, int64_t value) {
+    return guarded(h, [&] {
+        switch (option) {
+            case LFGPU_OPTION_WAIT_LIMIT_NS:
+                LF_REQUIRE(value > 0, LFGPU_ERR_ARGUMENT, "the wait limit must be positive");
+                h->wait_limit_ns = static_cast<unsigned long long>(value);
+                reset_status(*h);  // the limit travels in the device status word
+                LF_CUDA(cudaStreamSynchronize(h->stream));
+                break;
+            case LFGPU_OPTION_IC0_SWEEP:
+                LF_REQUIRE(value == LFGPU_IC0_SWEEP_AUTO || value == LFGPU_IC0_SWEEP_LEVELS ||
+                               value == LFGPU_IC0_SWEEP_POLLED,
+                           LFGPU_ERR_ARGUMENT, "ic0 sweep must be auto, levels or polled");
+                h->ic0_sweep = static_cast<int>(value);
+                break;
+            default:
+                throw Error{LFGPU_ERR_ARGUMENT, "unknown option"};
+        }
+    });
+}
+
 int lfgpu_set_mesh(lfgpu_t h, int64_t n_nodes, const double* xy, int64_t n_elements, const int32_t* element_nodes,
                    const int32_t* element_material, int64_t n_materials, const double* young, const double* poisson,
                    const double* thickness, int32_t plane_mode) {
@@ -562,9 +585,10 @@ lfgpu::PcgResult finish_in_fp64(lfgpu_t h, const lfgpu_solve_options* o, const l
     f.x0 = x0.p;
     f.max_iterations = std::max<i64>(1, s.max_iterations - done_iterations);
     float ms2 = 0.f;
-    const PcgResult r2 = f.precond == LFGPU_PRECOND_SUBDOMAIN ? run_pcg_separate(*h, f, &ms2, nullptr)
-                         : o->persistent                       ? run_pcg(*h, f, &ms2)
-                                                               : run_cg_graph(*h, f, &ms2);
+    const bool separate = f.precond == LFGPU_PRECOND_SUBDOMAIN || f.precond == LFGPU_PRECOND_IC0;
+    const PcgResult r2 = separate        ? run_pcg_separate(*h, f, &ms2, nullptr)
+                         : o->persistent ? run_pcg(*h, f, &ms2)
+                                         : run_cg_graph(*h, f, &ms2);
     *ms += ms2;
     return r2;
 }
@@ -584,8 +608,6 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
                    LFGPU_ERR_ARGUMENT, "preconditioner must be jacobi, block, ic0 or subdomain");
         LF_REQUIRE(o->precision == LFGPU_PRECISION_FP64 || o->precision == LFGPU_PRECISION_MIXED, LFGPU_ERR_ARGUMENT,
                    "precision must be fp64 or mixed");
-        LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner == LFGPU_PRECOND_IC0),
-                   LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi, block and subdomain preconditioners");
         lfgpu_report r{};
         r.status = LFGPU_OK;
         const double fnorm = device_norm2(*h, h->f, h->n);
@@ -612,13 +634,19 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
         if (o->preconditioner == LFGPU_PRECOND_IC0) {
             LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
             ensure_ic0(*h);
+            // The level schedules (once per pattern) and the factor in their order.
+            if (ic0_use_levels(*h, s.mixed)) ensure_ic0_sweep_values(*h, s.mixed);
             LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
             r.preconditioner_setup_ms = elapsed_ms(*h);
             if (o->storage == LFGPU_STORAGE_BSR) ensure_bsr(*h);
-            res = run_pcg_separate(*h, s, &ms, &apply_ms);
+            if (s.mixed) {
+                res = run_cg_graph(*h, s, &ms);
+            } else {
+                res = run_pcg_separate(*h, s, &ms, &apply_ms);
+                r.preconditioner_apply_ms = apply_ms;
+            }
             r.ic0_breakdowns = h->ic0_breakdowns;
             r.ic0_levels = h->ic0_levels;
-            r.preconditioner_apply_ms = apply_ms;
         } else if (o->preconditioner == LFGPU_PRECOND_SUBDOMAIN) {
             LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
             if (s.mixed) ensure_subdomain_inverse(*h);  // factor, then the FP32 block inverses
@@ -894,8 +922,6 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
             LF_REQUIRE(o != nullptr, LFGPU_ERR_ARGUMENT, "the adjoint solve needs solve options");
             LF_REQUIRE(o->preconditioner >= LFGPU_PRECOND_JACOBI && o->preconditioner <= LFGPU_PRECOND_SUBDOMAIN,
                        LFGPU_ERR_ARGUMENT, "preconditioner must be jacobi, block, ic0 or subdomain");
-            LF_REQUIRE(!(o->precision == LFGPU_PRECISION_MIXED && o->preconditioner == LFGPU_PRECOND_IC0),
-                       LFGPU_ERR_UNSUPPORTED, "mixed precision supports the jacobi, block and subdomain preconditioners");
             // Solve K lambda = dJ/du with dJ/du zeroed on the constrained DOFs: reuse the
             // solve machinery on the adjoint right-hand side.
             std::vector<double> rhs(dj_du, dj_du + n);
@@ -956,9 +982,12 @@ int lfgpu_adjoint(lfgpu_t h, const double* dj_du, const lfgpu_solve_options* o, 
         }
         g.ensure(64 + static_cast<size_t>(h->n_elem));
         double* gd = g.p + 64;
+        LF_CUDA(cudaEventRecord(h->ev_a, h->stream));
         launch_adjoint_grad(*h, h->u, lam, gd);
+        LF_CUDA(cudaEventRecord(h->ev_b, h->stream));
         LF_CUDA(cudaMemcpyAsync(grad, gd, sizeof(double) * h->n_elem, cudaMemcpyDeviceToHost, h->stream));
         check_status(*h);
+        h->timings.adjoint_kernel_ms = elapsed_ms(*h);
         if (rep) *rep = r;
     });
 }

@@ -29,6 +29,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 namespace lfgpu {
@@ -93,6 +94,17 @@ struct CgArgs {
     const double* sub_factor;
     const float* sub_inv32;        // mixed loop: block inverses, FP32 D x D squares
     const long long* sub_sq;       // offset of each subdomain's square
+    // IC(0) level-scheduled sweeps (ic0.cu builds the schedules): [0] forward, [1] backward
+    struct SweepPlan {
+        const int* level_begin;    // 2 per level + 2: first position, first entry
+        const int4* desc;          // per position: row, first entry, end entry, output index
+        const int* dep;            // per entry: position of the row it depends on
+        const void* val;           // factor entries in schedule order (double or float)
+        const void* inv;           // reciprocal pivots in schedule order
+        int levels;
+    } sw[2];
+    int sw_window;                 // ring slots per CTA (a power of two)
+    void* sw_y;                    // forward result in backward positions (double or float)
     int blocks;
     CgState* st;
     DeviceStatus* status;
@@ -307,8 +319,13 @@ __device__ __forceinline__ void bsr64_rows(const CgArgs& a, const G& g, Out&& ou
 // interior node's row cost one round of gather latency instead of three.  The
 // grid-stride loop loads the next row's block offsets while this row's blocks
 // stream, which takes one dependent load off each row's chain.
-template <typename G, typename Out>
-__device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& out) {
+//
+// Lanes 0 and 1 of each quad own DOFs 2 node and 2 node + 1 of the block row: each
+// loads its DOF's operands own(dof) before the row's blocks, so those loads overlap
+// the block stream instead of following it, and out(dof, row sum, operands) runs
+// on that lane.
+template <typename Own, typename G, typename Out>
+__device__ __forceinline__ void bsr32_rows(const CgArgs& a, const Own& own, const G& g, Out&& out) {
     const int lane = threadIdx.x & 31, sub = lane & 3;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int stride = ((gridDim.x * blockDim.x) >> 5) * 8;
@@ -325,6 +342,10 @@ __device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& ou
             nb_b = __ldg(a.brow + node + stride);
             nb_e = __ldg(a.brow + node + stride + 1);
         }
+        const int dof = 2 * node + (sub & 1);
+        const bool owner = act && sub < 2;
+        decltype(own(0)) mine{};
+        if (owner) mine = own(dof);
         float s0 = 0.f, s1 = 0.f;
         if (act) {
             // Columns as 16-bit offsets from the block row when they fit (half the bytes).
@@ -349,7 +370,7 @@ __device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& ou
         }
         s0 = quad_sum(s0);
         s1 = quad_sum(s1);
-        if (act && sub == 0) out(node, make_float2(s0, s1));
+        if (owner) out(dof, sub ? s1 : s0, mine);
     }
 }
 
@@ -586,11 +607,17 @@ __device__ __forceinline__ void pair_axpy(float& hi, float& lo, float ah, float 
     lo = __fsub_rn(l, __fsub_rn(hi, s));
 }
 
-// The subdomain preconditioner is applied by its own kernel (mx_sub_apply) after
-// mx_init and after every mx_update: those two leave z and r.z to it.
+// Preconditioners applied by their own kernels (the subdomain block solves,
+// mx_sub_apply; the IC(0) sweeps, ic0_level_sweep) run after mx_init and after
+// every mx_update: those two leave z and r.z to them.
+template <int PRECOND>
+constexpr bool applied_separately() {
+    return PRECOND == LFGPU_PRECOND_SUBDOMAIN || PRECOND == LFGPU_PRECOND_IC0;
+}
+
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
-    constexpr bool kSub = PRECOND == LFGPU_PRECOND_SUBDOMAIN;
+    constexpr bool kSub = applied_separately<PRECOND>();
     double v[2] = {0.0, 0.0};
     const double2* f2 = reinterpret_cast<const double2*>(a.f);
     float4* zp = reinterpret_cast<float4*>(a.zp0);
@@ -627,9 +654,17 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
     });
 }
 
+// The operands a product lane loads for its own DOF ahead of the row's blocks.
+struct DofOperands {
+    float2 zp;  // (z, p_old)
+    float hi, lo;
+};
+
 // q = K32 p with p = z + beta p_old formed on the fly; each row writes its p.
+// Eight CTAs per SM (32 registers a thread): the kernel is bound by load latency,
+// so every resident warp counts.
 template <int STORAGE>
-__global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
+__global__ void __launch_bounds__(kThreads, 8) mx_product(CgArgs a) {
     if (a.st->done) return;
     const float beta = a.st->beta32;
     const float4* zp4 = zp_buffer(a, a.st->it);
@@ -650,21 +685,25 @@ __global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
                        acc.add(pn * y);
                    });
     } else {
-        const float2* hi2 = reinterpret_cast<const float2*>(a.dhi);
-        const float2* lo2 = reinterpret_cast<const float2*>(a.dlo);
+        const float2* zp2 = reinterpret_cast<const float2*>(zp4);
         bsr32_rows(a,
+                   [&](int dof) {
+                       DofOperands o;
+                       o.zp = zp2[dof];
+                       o.hi = a.dhi[dof];
+                       o.lo = a.dlo[dof];
+                       return o;
+                   },
                    [&](int c) {
                        const float4 v = zp4[c];
                        return make_float2(pnew(v.x, v.y, beta), pnew(v.z, v.w, beta));
                    },
-                   [&](int node, float2 off) {
-                       const float4 v = zp4[node];
-                       const float2 pn = make_float2(pnew(v.x, v.y, beta), pnew(v.z, v.w, beta));
-                       const float2 h = hi2[node], l = lo2[node];
-                       const float2 y = make_float2(with_diag(off.x, h.x, l.x, pn.x), with_diag(off.y, h.y, l.y, pn.y));
-                       reinterpret_cast<float2*>(a.p32)[node] = pn;
-                       reinterpret_cast<float2*>(a.q32)[node] = y;
-                       acc.add(pn.x * y.x + pn.y * y.y);
+                   [&](int dof, float off, const DofOperands& o) {
+                       const float pn = pnew(o.zp.x, o.zp.y, beta);
+                       const float y = with_diag(off, o.hi, o.lo, pn);
+                       a.p32[dof] = pn;
+                       a.q32[dof] = y;
+                       acc.add(pn * y);
                    });
     }
     FloatPair v[1] = {acc};
@@ -685,7 +724,7 @@ __global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
 // x += alpha p (into the FP32 pair), r -= alpha q, z = M^-1 r; r.r and r.z.
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
-    constexpr bool kSub = PRECOND == LFGPU_PRECOND_SUBDOMAIN;
+    constexpr bool kSub = applied_separately<PRECOND>();
     if (a.st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_branch(a, false);
         return;
@@ -931,6 +970,268 @@ __global__ void __launch_bounds__(kSweepRows) ic0_backward(CgArgs a) {
     st_relaxed_gpu(reinterpret_cast<unsigned long long*>(a.z + row), out);
 }
 
+// ------------------------------------------------------------------ IC(0) level sweeps
+// The same two sweeps, scheduled by levels instead of polls: a row's level is one
+// more than the deepest row it depends on, so the rows of one level are
+// independent.  One cluster of kSweepCluster CTAs walks the levels in order; each
+// level's rows are split into one contiguous piece per CTA, one thread per row.
+//
+// Results travel through shared memory, not L2: every CTA keeps a ring of the last
+// sw_window results (slot = schedule position mod sw_window), and a thread that
+// finishes a row stores its result into every CTA's ring with st.async, which
+// also counts the bytes on that CTA's mbarrier of the level.  A CTA starts level L
+// once its mbarrier of level L - 1 has seen the whole level (width x size bytes),
+// so no cluster-wide barrier runs per level and the loads for the next levels stay
+// in flight across the wait: each thread loads the next level's row (descriptor,
+// right-hand side, pivot, the first kSweepRegEntries entries) into registers while
+// the current level runs, and the descriptor two levels ahead.  CTAs run at most
+// one level apart, so the ring spans the longest dependency distance plus two
+// levels (ensure_ic0_schedule checks it), and kSweepStages mbarriers cycle over the
+// levels; the warps of a CTA meet once per level, after the wait.  Waits are
+// bounded: on expiry the kernel records LFGPU_ERR_TIMEOUT and ends the solve.
+//
+// The arithmetic of a row is the polled sweeps': terms subtracted in the
+// reference's order, products and differences rounded separately, so the FP64
+// sweeps equal the reference's application bit for bit.  MODE 0 / 1: FP64 forward
+// (r -> y in backward order) / backward (-> z); MODE 2 / 3: the mixed loop's FP32
+// forward (r32) / backward, which writes z into the (z, p) copy the next product
+// reads and reduces r.z (rho and beta, as the subdomain application does).
+constexpr int kSweepRegEntries = 10;  // entries of a row held in registers (an interior Q4 row has at most 9)
+
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// Address of the same shared-memory variable in CTA `rank` of the cluster.
+__device__ __forceinline__ unsigned cluster_address(unsigned addr, unsigned rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void store_remote(unsigned addr, double v, unsigned bar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f64 [%0], %1, [%2];" ::"r"(addr), "d"(v),
+                 "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void store_remote(unsigned addr, float v, unsigned bar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f32 [%0], %1, [%2];" ::"r"(addr), "f"(v),
+                 "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ bool level_done(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for a level's results; false when it ran out (or another wait did).
+__device__ __forceinline__ bool wait_level(unsigned long long* bar, unsigned parity, DeviceStatus* status, int level) {
+    if (level_done(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (unsigned it = 1;; ++it) {
+        if (level_done(bar, parity)) return true;
+        if ((it & 15u) == 0u && wait_expired(status, t0, level)) return false;
+    }
+}
+
+__device__ __forceinline__ double sweep_term(double acc, double l, double v) { return __dsub_rn(acc, __dmul_rn(l, v)); }
+__device__ __forceinline__ float sweep_term(float acc, float l, float v) { return __fsub_rn(acc, __fmul_rn(l, v)); }
+__device__ __forceinline__ double sweep_scale(double acc, double inv) { return __dmul_rn(acc, inv); }
+__device__ __forceinline__ float sweep_scale(float acc, float inv) { return __fmul_rn(acc, inv); }
+
+// rho and beta from r.z after a separate preconditioner application (the mixed
+// loop's subdomain and IC(0) forms): the first rho after mx_init, then beta =
+// r.z / rho, or 0 after a residual replacement in restart mode.
+__device__ __forceinline__ void rho_from_application(const CgArgs& a, const double* t) {
+    CgState* st = a.st;
+    const bool first = st->it == 0;
+    if (!(t[0] > 0.0) || !isfinite(t[0])) {
+        st->status = first ? LFGPU_ERR_RHO_INITIAL : LFGPU_ERR_RHO;
+        st->done = 1;
+    } else {
+        st->beta = (first || (a.restart && st->refine)) ? 0.0 : t[0] / st->rho;
+        st->beta32 = static_cast<float>(st->beta);
+        st->rho = t[0];
+    }
+    set_loop(a, !st->done);
+}
+
+template <typename T>
+struct SweepRow {
+    int pos;   // schedule position, -1: none
+    int4 d;    // row, first entry, end entry, output index
+    T rhs, inv, r;
+    int dep[kSweepRegEntries];
+    T val[kSweepRegEntries];
+};
+
+template <int MODE>
+__global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepThreads) ic0_level_sweep(CgArgs a) {
+    using T = typename std::conditional<(MODE < 2), double, float>::type;
+    constexpr bool kFwd = (MODE & 1) == 0;
+    constexpr bool kMixed = MODE >= 2;
+    constexpr int S = kSweepStages;
+    constexpr int E = kSweepRegEntries;
+    if (a.st->done) return;  // read before the kernel changes anything: the same in every CTA
+    extern __shared__ __align__(16) unsigned char sweep_smem[];
+    __shared__ __align__(8) unsigned long long bars[S];
+    __shared__ int s_failed;
+    T* ring = reinterpret_cast<T*>(sweep_smem);
+    const CgArgs::SweepPlan& sp = a.sw[kFwd ? 0 : 1];
+    const int* __restrict__ lvl = sp.level_begin;
+    const int4* __restrict__ desc = sp.desc;
+    const int* __restrict__ dep = sp.dep;
+    const T* __restrict__ val = static_cast<const T*>(sp.val);
+    const T* __restrict__ pinv = static_cast<const T*>(sp.inv);
+    T* yb = static_cast<T*>(a.sw_y);
+    const int levels = sp.levels;
+    const int mask = a.sw_window - 1;
+    const unsigned rank = cluster_rank();
+    const int tid = threadIdx.x;
+    auto width_bytes = [&](int L) { return static_cast<unsigned>(__ldg(lvl + 2 * L + 2) - __ldg(lvl + 2 * L)) * sizeof(T); };
+    if (tid == 0) {
+        s_failed = 0;
+        for (int s = 0; s < S; ++s) mbar_init(bars + s, 1);
+        mbar_init_fence();
+        for (int L = 0; L < S && L < levels; ++L) mbar_expect_tx(bars + L, width_bytes(L));
+    }
+    cluster_sync_all();  // every CTA's mbarriers are armed before any result arrives
+    unsigned ring_at[kSweepCluster], bar_at[kSweepCluster];
+#pragma unroll
+    for (int k = 0; k < kSweepCluster; ++k) {
+        ring_at[k] = cluster_address(smem_u32(ring), k);
+        bar_at[k] = cluster_address(smem_u32(bars), k);
+    }
+    // This thread's first position in level L and the end of this CTA's piece.
+    auto piece = [&](int L, int& p, int& end) {
+        const int p0 = __ldg(lvl + 2 * L), p1 = __ldg(lvl + 2 * L + 2);
+        const int chunk = (p1 - p0 + kSweepCluster - 1) / kSweepCluster;
+        const int first = p0 + static_cast<int>(rank) * chunk;
+        end = min(p1, first + chunk);
+        p = first + tid;
+    };
+    auto rhs_of = [&](int p, int row) -> T {
+        if constexpr (!kFwd) return yb[p];
+        else if constexpr (kMixed) return a.r32[row];
+        else return a.r[row];
+    };
+    auto load_row = [&](SweepRow<T>& w, int p, int4 d) {
+        w.pos = p;
+        w.d = d;
+        if (p < 0) return;
+        w.rhs = rhs_of(p, d.x);
+        w.inv = __ldg(pinv + p);
+        if constexpr (MODE == 3) w.r = a.r32[d.x];
+#pragma unroll
+        for (int k = 0; k < E; ++k) {
+            if (d.y + k < d.z) {
+                w.dep[k] = __ldg(dep + d.y + k);
+                w.val[k] = __ldg(val + d.y + k);
+            }
+        }
+    };
+    FloatPair rz;
+    auto finish_row = [&](int p, int4 d, T rhs, T inv, T r, const int* dk, const T* vk, int L) {
+        T acc = rhs;
+#pragma unroll
+        for (int k = 0; k < E; ++k)
+            if (d.y + k < d.z) acc = sweep_term(acc, vk[k], ring[dk[k] & mask]);
+        for (int j = d.y + E; j < d.z; ++j) acc = sweep_term(acc, __ldg(val + j), ring[__ldg(dep + j) & mask]);
+        const T y = sweep_scale(acc, inv);
+        const unsigned slot = static_cast<unsigned>(p & mask) * sizeof(T);
+        const unsigned bar = static_cast<unsigned>(L % S) * 8u;
+#pragma unroll
+        for (int k = 0; k < kSweepCluster; ++k) store_remote(ring_at[k] + slot, y, bar_at[k] + bar);
+        if constexpr (kFwd) {
+            yb[d.w] = y;
+        } else if constexpr (!kMixed) {
+            a.z[d.x] = y;
+        } else {
+            // z of DOF 2m sits in .x of node m's (z, p) float4, z of DOF 2m + 1 in .z.
+            reinterpret_cast<float*>(zp_buffer(a, a.st->it))[4 * (d.x >> 1) + 2 * (d.x & 1)] = y;
+            rz.add(r * y);
+        }
+    };
+    const int4 none = make_int4(0, 0, 0, 0);
+    SweepRow<T> cur, nxt;
+    int4 d1 = none, d2 = none;
+    int p1 = -1, p2 = -1;
+    {
+        int p, end;
+        piece(0, p, end);
+        load_row(cur, p < end ? p : -1, p < end ? __ldg(desc + p) : none);
+        if (levels > 1) {
+            piece(1, p, end);
+            p1 = p < end ? p : -1;
+            if (p1 >= 0) d1 = __ldg(desc + p1);
+        }
+    }
+    bool ok = true;
+    for (int L = 0; L < levels; ++L) {
+        // Loads for the next levels, issued before this level's wait.
+        p2 = -1;
+        if (L + 2 < levels) {
+            int p, end;
+            piece(L + 2, p, end);
+            if (p < end) {
+                p2 = p;
+                d2 = __ldg(desc + p);
+            }
+        }
+        if (L + 1 < levels) load_row(nxt, p1, d1);
+        if (L > 0) {
+            const int prev = L - 1;
+            ok = wait_level(bars + prev % S, static_cast<unsigned>(prev / S) & 1u, a.status, prev) && ok;
+            // Every thread of the CTA has seen level prev complete: its mbarrier is
+            // free again, armed for level prev + S.  (This also keeps the CTA's warps
+            // on one level, so no thread polls a phase that has moved on.)
+            __syncthreads();
+            if (tid == 0 && prev + S < levels) mbar_expect_tx(bars + prev % S, width_bytes(prev + S));
+        }
+        if (cur.pos >= 0) finish_row(cur.pos, cur.d, cur.rhs, cur.inv, cur.r, cur.dep, cur.val, L);
+        // Levels wider than the cluster's threads: further rows, loaded here.
+        {
+            int p, end;
+            piece(L, p, end);
+            for (p += kSweepThreads; p < end; p += kSweepThreads) {
+                SweepRow<T> w;
+                load_row(w, p, __ldg(desc + p));
+                finish_row(w.pos, w.d, w.rhs, w.inv, w.r, w.dep, w.val, L);
+            }
+        }
+        cur = nxt;
+        if (L + 1 >= levels) cur.pos = -1;
+        p1 = p2;
+        d1 = d2;
+    }
+    // Every result bound for this CTA has arrived before it exits.
+    if (levels > 0)
+        ok = wait_level(bars + (levels - 1) % S, static_cast<unsigned>((levels - 1) / S) & 1u, a.status, levels - 1) &&
+             ok;
+    if (!ok) s_failed = 1;
+    __syncthreads();
+    if (s_failed) {
+        // A wait ran out: end the solve (the status word already says why).
+        if (tid == 0) {
+            a.st->status = LFGPU_ERR_TIMEOUT;
+            a.st->done = 1;
+            set_loop(a, false);
+        }
+        return;
+    }
+    if constexpr (MODE == 3) {
+        FloatPair vv[1] = {rz};
+        reduce_last<1>(a, 2, vv, [&](const double* t) { rho_from_application(a, t); });
+    }
+}
+
 __device__ __forceinline__ void ic0_mark_pending(const CgArgs& a, int i) {
     if (a.y == nullptr) return;  // the subdomain preconditioner writes z without polls
     const double pending = __longlong_as_double(static_cast<long long>(kPending));
@@ -1129,19 +1430,7 @@ __global__ void __launch_bounds__(LFGPU_SUBDOMAIN_MAX_DOFS) mx_sub_apply(CgArgs 
         rz.add(r * x);
     }
     FloatPair vv[1] = {rz};
-    reduce_last<1>(a, 2, vv, [&](const double* t) {
-        CgState* st = a.st;
-        const bool first = st->it == 0;
-        if (!(t[0] > 0.0) || !isfinite(t[0])) {
-            st->status = first ? LFGPU_ERR_RHO_INITIAL : LFGPU_ERR_RHO;
-            st->done = 1;
-        } else {
-            st->beta = (first || (a.restart && st->refine)) ? 0.0 : t[0] / st->rho;
-            st->beta32 = static_cast<float>(st->beta);
-            st->rho = t[0];
-        }
-        set_loop(a, !st->done);
-    });
+    reduce_last<1>(a, 2, vv, [&](const double* t) { rho_from_application(a, t); });
 }
 
 // One FP64 application of the Jacobi or 2x2 nodal preconditioner.
@@ -1203,19 +1492,32 @@ void build_fp64(cudaGraph_t g, CgArgs* a, int blocks) {
 
 constexpr int kBodyIterations = 8;
 
-// The subdomain preconditioner (sub_grid CTAs of sub_threads) adds its own kernel
-// after mx_init and after each iteration's IF node; the branch then holds only
-// the flush and the FP64 residual, as the kernel after it re-preconditions.
+// The mixed loop's separately applied preconditioners, after `dep`; returns the
+// last node.  Subdomain: one kernel (sub_grid CTAs of sub_threads); IC(0): the
+// forward and the backward FP32 level sweep (one cluster each, smem bytes of ring).
+template <int PRECOND>
+cudaGraphNode_t add_mixed_apply(cudaGraph_t g, cudaGraphNode_t dep, CgArgs* a, int sub_grid, int sub_threads,
+                                int smem) {
+    cudaGraphNode_t n1, n2;
+    if constexpr (PRECOND == LFGPU_PRECOND_SUBDOMAIN) {
+        add_kernel(g, &n1, &dep, 1, mx_sub_apply, sub_grid, a, 0, sub_threads);
+        return n1;
+    } else {
+        add_kernel(g, &n1, &dep, 1, ic0_level_sweep<2>, kSweepCluster, a, smem, kSweepThreads);
+        add_kernel(g, &n2, &n1, 1, ic0_level_sweep<3>, kSweepCluster, a, smem, kSweepThreads);
+        return n2;
+    }
+}
+
+// Preconditioners applied by their own kernels add them after mx_init and after
+// each iteration's IF node; the branch then holds only the flush and the FP64
+// residual, as the kernels after it re-precondition.
 template <int STORAGE, int PRECOND>
-void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub_threads = 0) {
-    constexpr bool kSub = PRECOND == LFGPU_PRECOND_SUBDOMAIN;
+void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub_threads = 0, int smem = 0) {
+    constexpr bool kSub = applied_separately<PRECOND>();
     cudaGraphNode_t n_init;
     add_kernel(g, &n_init, nullptr, 0, mx_init<PRECOND>, blocks, a);
-    if constexpr (kSub) {
-        cudaGraphNode_t n_apply;
-        add_kernel(g, &n_apply, &n_init, 1, mx_sub_apply, sub_grid, a, 0, sub_threads);
-        n_init = n_apply;
-    }
+    if constexpr (kSub) n_init = add_mixed_apply<PRECOND>(g, n_init, a, sub_grid, sub_threads, smem);
     cudaGraph_t body;
     const cudaGraphNode_t n_loop = add_conditional(g, &n_init, 1, a->loop, cudaGraphCondTypeWhile, &body);
     cudaGraphNode_t n_flush;
@@ -1238,8 +1540,7 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub
         add_kernel(branch, &k3, nullptr, 0, mx_flush<false>, blocks, ah);
         add_kernel(branch, &k4, &k3, 1, mx_residual<STORAGE>, blocks, ah);
         if constexpr (kSub) {
-            add_kernel(body, &k5, &prev, 1, mx_sub_apply, sub_grid, ah, 0, sub_threads);
-            prev = k5;
+            prev = add_mixed_apply<PRECOND>(body, prev, ah, sub_grid, sub_threads, smem);
         } else {
             add_kernel(branch, &k5, &k4, 1, mx_reprecondition<PRECOND>, blocks, ah);
         }
@@ -1284,15 +1585,22 @@ struct EventTrail {
 // replacement, 3 mixed re-preconditioning (subdomain: the block solves).
 template <int STORAGE, int PRECOND>
 void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int iters, EventTrail& trail,
-                     int sub_grid = 0, int sub_threads = 0) {
-    constexpr bool kSub = PRECOND == LFGPU_PRECOND_SUBDOMAIN;
+                     int sub_grid = 0, int sub_threads = 0, int smem = 0) {
+    constexpr bool kSub = applied_separately<PRECOND>();
     auto chain = [&](auto kernel, int phase) {
         kernel<<<blocks, kThreads, 0, stream>>>(*a);
         LF_CUDA(cudaGetLastError());
         trail.mark(phase);
     };
     auto sub_apply = [&](int phase) {
-        mx_sub_apply<<<sub_grid, sub_threads, 0, stream>>>(*a);
+        if constexpr (PRECOND == LFGPU_PRECOND_IC0) {
+            ic0_level_sweep<2><<<kSweepCluster, kSweepThreads, smem, stream>>>(*a);
+            LF_CUDA(cudaGetLastError());
+            trail.mark(phase);
+            ic0_level_sweep<3><<<kSweepCluster, kSweepThreads, smem, stream>>>(*a);
+        } else {
+            mx_sub_apply<<<sub_grid, sub_threads, 0, stream>>>(*a);
+        }
         LF_CUDA(cudaGetLastError());
         trail.mark(phase);
     };
@@ -1323,9 +1631,11 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
 // subdomain) in place of the two sweeps.
 struct SeparateApply {
     bool subdomain;
-    int chunks;    // IC(0): row chunks of the sweeps
+    int chunks;    // IC(0): row chunks of the polled sweeps
     int sub_grid;  // subdomain: subdomains, and threads per CTA
     int sub_threads;
+    bool levels;   // IC(0): the level-scheduled sweeps, with this much shared memory per CTA
+    int smem;
 };
 
 // Adds the application after `dep`; returns its last node.
@@ -1334,6 +1644,11 @@ cudaGraphNode_t add_apply(cudaGraph_t g, cudaGraphNode_t dep, CgArgs* a, const S
     if (ap.subdomain) {
         add_kernel(g, &n1, &dep, 1, subdomain_apply, ap.sub_grid, a, 0, ap.sub_threads);
         return n1;
+    }
+    if (ap.levels) {
+        add_kernel(g, &n1, &dep, 1, ic0_level_sweep<0>, kSweepCluster, a, ap.smem, kSweepThreads);
+        add_kernel(g, &n2, &n1, 1, ic0_level_sweep<1>, kSweepCluster, a, ap.smem, kSweepThreads);
+        return n2;
     }
     add_kernel(g, &n1, &dep, 1, ic0_forward, ap.chunks, a, 0, kSweepRows);
     add_kernel(g, &n2, &n1, 1, ic0_backward, ap.chunks, a, 0, kSweepRows);
@@ -1374,10 +1689,18 @@ void launch_separate_unrolled(cudaStream_t stream, CgArgs* a, int blocks, const 
             trail.mark(in_loop ? 2 : -1);
             return;
         }
-        ic0_forward<<<ap.chunks, kSweepRows, 0, stream>>>(*a);  // one CTA per chunk of kSweepRows rows
+        if (ap.levels) {
+            ic0_level_sweep<0><<<kSweepCluster, kSweepThreads, ap.smem, stream>>>(*a);
+        } else {
+            ic0_forward<<<ap.chunks, kSweepRows, 0, stream>>>(*a);  // one CTA per chunk of kSweepRows rows
+        }
         LF_CUDA(cudaGetLastError());
         trail.mark(in_loop ? 2 : -1);
-        ic0_backward<<<ap.chunks, kSweepRows, 0, stream>>>(*a);
+        if (ap.levels) {
+            ic0_level_sweep<1><<<kSweepCluster, kSweepThreads, ap.smem, stream>>>(*a);
+        } else {
+            ic0_backward<<<ap.chunks, kSweepRows, 0, stream>>>(*a);
+        }
         LF_CUDA(cudaGetLastError());
         trail.mark(in_loop ? 3 : -1);
     };
@@ -1406,6 +1729,38 @@ SeparateApply subdomain_args(Context& c, CgArgs& a) {
     ap.subdomain = true;
     ap.sub_grid = static_cast<int>(c.sub_count);
     ap.sub_threads = std::max(32, (c.sub_max + 31) / 32 * 32);
+    return ap;
+}
+
+// The level-scheduled IC(0) sweeps' arrays (fp32: the mixed loop's FP32 factor),
+// with the kernels' shared-memory allowance raised to the ring.  Requires
+// ensure_ic0, ensure_ic0_schedule and ensure_ic0_sweep_values.
+SeparateApply sweep_args(Context& c, CgArgs& a, bool fp32) {
+    for (int d = 0; d < 2; ++d) {
+        const Context::Sweep& s = c.sweep[d];
+        a.sw[d].level_begin = s.level_begin;
+        a.sw[d].desc = s.desc;
+        a.sw[d].dep = s.dep;
+        a.sw[d].val = fp32 ? static_cast<const void*>(s.val32.p) : static_cast<const void*>(s.val.p);
+        a.sw[d].inv = fp32 ? static_cast<const void*>(s.inv32.p) : static_cast<const void*>(s.inv.p);
+        a.sw[d].levels = s.levels;
+    }
+    a.sw_window = c.sweep_window;
+    SeparateApply ap{};
+    ap.levels = true;
+    if (fp32) {
+        c.sweep_y32.ensure(c.n);
+        a.sw_y = c.sweep_y32.p;
+        ap.smem = c.sweep_window * static_cast<int>(sizeof(float));
+        LF_CUDA(cudaFuncSetAttribute(ic0_level_sweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ap.smem));
+        LF_CUDA(cudaFuncSetAttribute(ic0_level_sweep<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, ap.smem));
+    } else {
+        c.sweep_y.ensure(c.n);
+        a.sw_y = c.sweep_y.p;
+        ap.smem = c.sweep_window * static_cast<int>(sizeof(double));
+        LF_CUDA(cudaFuncSetAttribute(ic0_level_sweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, ap.smem));
+        LF_CUDA(cudaFuncSetAttribute(ic0_level_sweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ap.smem));
+    }
     return ap;
 }
 
@@ -1467,11 +1822,17 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         a.dlo = c.diag_lo;
     }
     const bool sub = s.precond == LFGPU_PRECOND_SUBDOMAIN;
-    LF_REQUIRE(!sub || s.mixed, LFGPU_ERR_ARGUMENT, "the FP64 subdomain solve is run_pcg_separate");
+    const bool ic = s.precond == LFGPU_PRECOND_IC0;
+    LF_REQUIRE(!(sub || ic) || s.mixed, LFGPU_ERR_ARGUMENT, "the FP64 subdomain and ic0 solves are run_pcg_separate");
     SeparateApply ap{};
     if (sub) {
         ensure_subdomain_inverse(c);  // no-op when the solve's setup built it
         ap = subdomain_args(c, a);
+    } else if (ic) {
+        ensure_ic0(c);  // no-op when the solve's setup built them
+        ic0_use_levels(c, true);
+        ensure_ic0_sweep_values(c, true);
+        ap = sweep_args(c, a, true);
     }
     // Reduction partials: one per CTA of the widest reducing launch (the subdomain
     // kernel runs a CTA per subdomain).
@@ -1503,6 +1864,12 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         else if (sub)
             launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_SUBDOMAIN>(c.stream, &a, blocks, mx, s.unrolled, trail,
                                                                         ap.sub_grid, ap.sub_threads);
+        else if (ic && csr)
+            launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_IC0>(c.stream, &a, blocks, mx, s.unrolled, trail, 0, 0,
+                                                                  ap.smem);
+        else if (ic)
+            launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_IC0>(c.stream, &a, blocks, mx, s.unrolled, trail, 0, 0,
+                                                                  ap.smem);
         else if (csr && jac) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
         else if (csr) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled, trail);
         else if (jac) launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
@@ -1526,6 +1893,10 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
             build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_SUBDOMAIN>(gb.graph, &a, blocks, ap.sub_grid, ap.sub_threads);
         else if (sub)
             build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_SUBDOMAIN>(gb.graph, &a, blocks, ap.sub_grid, ap.sub_threads);
+        else if (ic && csr)
+            build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_IC0>(gb.graph, &a, blocks, 0, 0, ap.smem);
+        else if (ic)
+            build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_IC0>(gb.graph, &a, blocks, 0, 0, ap.smem);
         else if (csr && jac) build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
         else if (csr) build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
         else if (jac) build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
@@ -1552,7 +1923,14 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     // of every pass.
     // IC(0): residual (warm start), init, two sweeps and start, then six kernels a
     // pass; subdomain block-Jacobi: one apply kernel in place of the two sweeps.
-    if (s.precond == LFGPU_PRECOND_IC0)
+    if (s.precond == LFGPU_PRECOND_IC0 && s.mixed)  // mixed: init + two sweeps, then product, update and two
+                                                    // sweeps an iteration, flush and residual per replacement,
+                                                    // final flush
+        c.launches += 3 + (s.unrolled > 0 ? 6 * static_cast<i64>(s.unrolled)
+                                          : 4 * kBodyIterations * ((st.it + kBodyIterations - 1) / kBodyIterations) +
+                                                2 * st.refs) +
+                      1;
+    else if (s.precond == LFGPU_PRECOND_IC0)
         c.launches += (s.x0 ? 1 : 0) + 4 + 6 * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
     else if (s.precond == LFGPU_PRECOND_SUBDOMAIN && !s.mixed)
         c.launches += (s.x0 ? 1 : 0) + 3 + 5 * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
@@ -1626,6 +2004,9 @@ PcgResult run_pcg_separate(Context& c, const SolveSetup& s, float* kernel_ms, do
     SeparateApply ap{};
     if (sub) {
         ap = subdomain_args(c, a);
+    } else if (ic0_use_levels(c, false)) {
+        ensure_ic0_sweep_values(c, false);
+        ap = sweep_args(c, a, false);  // no pending marks, no chunk counters: a.y and a.ic_chunks stay null
     } else {
         a.y = c.v64[4];
         ic0_args(c, a);
@@ -1694,7 +2075,18 @@ void launch_precond_apply(Context& c, int precond, const double* r, double* z) {
     a.status = c.status;
     a.invd64 = c.inv_diag64;
     a.blk64 = c.blk64;
-    if (precond == LFGPU_PRECOND_IC0) {
+    if (precond == LFGPU_PRECOND_IC0 && ic0_use_levels(c, false)) {
+        // The sweeps read the done flag of a solver state: give them a fresh one.
+        c.cg_state.ensure(sizeof(CgState));
+        a.st = reinterpret_cast<CgState*>(c.cg_state.p);
+        LF_CUDA(cudaMemsetAsync(c.cg_state.p, 0, sizeof(CgState), c.stream));
+        ensure_ic0_sweep_values(c, false);
+        const SeparateApply ap = sweep_args(c, a, false);
+        ic0_level_sweep<0><<<kSweepCluster, kSweepThreads, ap.smem, c.stream>>>(a);
+        LF_CUDA(cudaGetLastError());
+        ic0_level_sweep<1><<<kSweepCluster, kSweepThreads, ap.smem, c.stream>>>(a);
+        c.launches += 2;
+    } else if (precond == LFGPU_PRECOND_IC0) {
         // The sweeps read the done flag of a solver state: give them a fresh one.
         c.cg_state.ensure(sizeof(CgState));
         a.st = reinterpret_cast<CgState*>(c.cg_state.p);

@@ -60,6 +60,10 @@ struct Buf {
     operator T*() const { return p; }
 };
 
+// A wait that gives up after DeviceStatus::wait_limit_ns sets DeviceStatus::abort
+// and returns.  The default limit; a handle can set another (lfgpu_set_option).
+constexpr unsigned long long kWaitLimitNs = 4000000000ull;  // 4 s
+
 // Device-side status word of one handle.  Kernels record the first failure here;
 // the host reads it after the stream synchronises.
 struct DeviceStatus {
@@ -67,6 +71,8 @@ struct DeviceStatus {
     int bad_index;       // element, row or block that caused it (smallest wins)
     unsigned int abort;  // set when any CTA gives up a wait; every wait checks it
     int pad;
+    unsigned long long wait_limit_ns;  // how long a bounded wait may spin (the handle's option)
+    unsigned long long pad2;
 };
 
 // Result record the persistent PCG kernels write (CTA 0) at exit.
@@ -224,6 +230,28 @@ struct Context {
     int sub_max = 0;  // DOFs of the largest subdomain
     double sub_capture = 0.0;
 
+    // IC(0) level schedules of the two sweeps (per pattern version) and the factor
+    // in schedule order (per K version; an FP32 copy once a mixed solve asks).
+    struct Sweep {
+        int levels = 0, entries = 0;
+        Buf<int> level_begin;  // 2 per level + 2: first position, first entry
+        Buf<int4> desc;        // per position: row, first entry, end entry, output index
+        Buf<int> dep;          // per entry: position of the row it depends on
+        Buf<double> val, inv;  // factor entries and reciprocal pivots in schedule order
+        Buf<float> val32, inv32;
+        unsigned long long val_version = ~0ull, val32_version = ~0ull;
+    };
+    Sweep sweep[2];                   // forward, backward
+    unsigned long long sweep_pattern_version = ~0ull;
+    int sweep_window = 0;             // ring slots (a power of two); 0: the schedule does not fit
+    i64 sweep_max_width = 0, sweep_max_distance = 0;
+    Buf<double> sweep_y;              // forward result, in backward positions
+    Buf<float> sweep_y32;
+
+    // Options (lfgpu_set_option).
+    unsigned long long wait_limit_ns = kWaitLimitNs;
+    int ic0_sweep = LFGPU_IC0_SWEEP_AUTO;
+
     lfgpu_timings timings{};
     i64 launches = 0;                 // kernels launched by this handle (graph nodes included)
     cudaEvent_t user_ev[8] = {};      // lfgpu_event_record slots
@@ -261,8 +289,6 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// A wait that gives up after this long sets DeviceStatus::abort and returns.
-constexpr unsigned long long kWaitLimitNs = 4000000000ull;  // 4 s
 
 // GPU-scope accesses for values and flags that other CTAs poll while a kernel runs.
 __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
@@ -291,7 +317,7 @@ __device__ __forceinline__ unsigned ld_relaxed_gpu(const unsigned* p) {
 // limit ran out (then this wait records LFGPU_ERR_TIMEOUT and sets the abort flag).
 __device__ __forceinline__ bool wait_expired(DeviceStatus* status, unsigned long long t0, int index) {
     if (ld_relaxed_gpu(&status->abort) != 0u) return true;
-    if (global_ns() - t0 > kWaitLimitNs) {
+    if (global_ns() - t0 > status->wait_limit_ns) {
         atomicExch(&status->abort, 1u);
         record_failure(status, LFGPU_ERR_TIMEOUT, index);
         return true;
@@ -320,7 +346,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned long long* counter, unsign
                 ok = 0;
                 break;
             }
-            if (global_ns() - start > kWaitLimitNs) {
+            if (global_ns() - start > status->wait_limit_ns) {
                 atomicExch(&status->abort, 1u);
                 record_failure(status, LFGPU_ERR_TIMEOUT, static_cast<int>(blockIdx.x));
                 ok = 0;

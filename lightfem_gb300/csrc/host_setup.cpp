@@ -8,6 +8,9 @@
 //   greedy_colors   element_colors, src/solver.cpp:100-133
 //   rcm_order       reverse_cuthill_mckee, src/reordering.cpp:11-62
 //   subdomain_split split_by_chunks / split_by_coordinates, src/precond.cpp:19-105
+//   sweep_schedule  level schedule of IncompleteCholesky0::apply's two sweeps,
+//                   src/precond.cpp:386-412 (no counterpart: the reference sweeps
+//                   serially)
 //
 // A Q4 element couples both DOFs of each of its nodes, so rows 2i and 2i+1 share
 // one column list {2j, 2j+1 : j in S(i)} where S(i) is the set of nodes sharing an
@@ -248,6 +251,77 @@ long long subdomain_split(long long n_nodes, const double* xy, long long per, bo
     for (size_t s = 0; s < spans.size(); ++s)
         for (size_t k = spans[s].first; k < spans[s].last; ++k) owner[perm[k]] = static_cast<uint32_t>(s);
     return static_cast<long long>(spans.size());
+}
+
+void sweep_schedule(int n, const int* rowptr, const int* col, const int* diag, bool forward, SweepSchedule& s) {
+    if (n < 0) throw std::invalid_argument("sweep_schedule: negative size");
+    // Level of every row: forward rows ascending (dependencies are smaller rows),
+    // backward rows descending (dependencies are larger rows).
+    std::vector<int> level(static_cast<size_t>(n), 0);
+    int levels = 0;
+    auto visit = [&](int r) {
+        int lv = 0;
+        const int b = forward ? rowptr[r] : diag[r] + 1;
+        const int e = forward ? diag[r] : rowptr[r + 1];
+        for (int k = b; k < e; ++k) lv = std::max(lv, level[static_cast<size_t>(col[k])] + 1);
+        level[static_cast<size_t>(r)] = lv;
+        levels = std::max(levels, lv + 1);
+    };
+    if (forward) {
+        for (int r = 0; r < n; ++r) visit(r);
+    } else {
+        for (int r = n - 1; r >= 0; --r) visit(r);
+    }
+    s.levels = levels;
+    // Positions: counting sort by level, rows ascending (forward) or descending
+    // (backward) within a level.
+    std::vector<int> count(static_cast<size_t>(levels) + 1, 0);
+    for (int r = 0; r < n; ++r) ++count[static_cast<size_t>(level[static_cast<size_t>(r)]) + 1];
+    s.max_width = 0;
+    for (int l = 0; l < levels; ++l) s.max_width = std::max(s.max_width, count[static_cast<size_t>(l) + 1]);
+    for (int l = 0; l < levels; ++l) count[static_cast<size_t>(l) + 1] += count[static_cast<size_t>(l)];
+    std::vector<int> fill(count.begin(), count.end() - 1);
+    std::vector<int> order(static_cast<size_t>(n));
+    s.position.assign(static_cast<size_t>(n), 0);
+    for (int i = 0; i < n; ++i) {
+        const int r = forward ? i : n - 1 - i;
+        const int p = fill[static_cast<size_t>(level[static_cast<size_t>(r)])]++;
+        order[static_cast<size_t>(p)] = r;
+        s.position[static_cast<size_t>(r)] = p;
+    }
+    // Entries in schedule order; each row's entries in the reference's order.
+    s.desc.assign(4 * static_cast<size_t>(n), 0);
+    long long entries = 0;
+    for (int r = 0; r < n; ++r) entries += forward ? diag[r] - rowptr[r] : rowptr[r + 1] - diag[r] - 1;
+    if (entries > 2147483647LL) throw std::invalid_argument("sweep_schedule: too many entries");
+    s.dep.assign(static_cast<size_t>(entries), 0);
+    s.level_begin.assign(2 * (static_cast<size_t>(levels) + 1), 0);
+    int j = 0;
+    int l = 0;
+    s.max_distance = 0;
+    for (int p = 0; p < n; ++p) {
+        const int r = order[static_cast<size_t>(p)];
+        while (l < levels && count[static_cast<size_t>(l)] == p) {  // first position of level l
+            s.level_begin[2 * static_cast<size_t>(l)] = p;
+            s.level_begin[2 * static_cast<size_t>(l) + 1] = j;
+            ++l;
+        }
+        const int jb = j;
+        if (forward) {
+            for (int k = rowptr[r]; k < diag[r]; ++k) s.dep[static_cast<size_t>(j++)] = s.position[static_cast<size_t>(col[k])];
+        } else {
+            for (int k = rowptr[r + 1] - 1; k > diag[r]; --k)
+                s.dep[static_cast<size_t>(j++)] = s.position[static_cast<size_t>(col[k])];
+        }
+        for (int t = jb; t < j; ++t)
+            s.max_distance = std::max<long long>(s.max_distance, p - s.dep[static_cast<size_t>(t)]);
+        s.desc[4 * static_cast<size_t>(p)] = r;
+        s.desc[4 * static_cast<size_t>(p) + 1] = jb;
+        s.desc[4 * static_cast<size_t>(p) + 2] = j;
+        s.desc[4 * static_cast<size_t>(p) + 3] = r;
+    }
+    s.level_begin[2 * static_cast<size_t>(levels)] = n;
+    s.level_begin[2 * static_cast<size_t>(levels) + 1] = j;
 }
 
 }  // namespace lfgpu

@@ -16,11 +16,19 @@
 // proceeds as soon as its dependencies are done -- no level schedule.  Each row is
 // computed by one thread in the reference's operation order without contraction,
 // so the factor equals the reference's bit for bit.
+//
+// Level schedules.  The triangular sweeps (cg_graph.cu) can also run level by
+// level: sweep_schedule (host_setup.cpp) lists the rows of each sweep level by
+// level, and ensure_ic0_sweep_values copies the factor into that order, so the
+// entries a level needs are contiguous.  The forward sweep writes its result in
+// the backward sweep's order, so the backward sweep reads it contiguously.
 #include "common.cuh"
+#include "host_setup.hpp"
 #include "kernels.hpp"
 
 #include <climits>
 #include <cmath>
+#include <thread>
 
 namespace lfgpu {
 namespace {
@@ -194,6 +202,118 @@ void ensure_ic0(Context& c) {
     // The forward and the backward sweep each have (longest chain + 1) levels.
     c.ic0_levels = 2 * (static_cast<i64>(misc[kIc0MaxLevel]) + 1);
     c.ic0_version = c.k_version;
+}
+
+// ------------------------------------------------------------------ level schedules
+namespace {
+
+// Factor entries and reciprocal pivots in schedule order: forward entries are
+// row r's columns left of its diagonal, ascending; backward entries row c's
+// columns right of its diagonal, descending (the L(c, r) the transpose stored there).
+template <typename T>
+__global__ void ic0_schedule_values_kernel(int n, bool forward, const int4* __restrict__ desc,
+                                           const int* __restrict__ rowptr, const int* __restrict__ diag,
+                                           const double* __restrict__ F, const double* __restrict__ inv,
+                                           T* __restrict__ val, T* __restrict__ pinv) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int4 d = desc[p];
+        const int row = d.x;
+        if (forward) {
+            const int b = rowptr[row];
+            for (int j = d.y; j < d.z; ++j) val[j] = static_cast<T>(F[b + (j - d.y)]);
+        } else {
+            const int top = rowptr[row + 1] - 1;
+            for (int j = d.y; j < d.z; ++j) val[j] = static_cast<T>(F[top - (j - d.y)]);
+        }
+        pinv[p] = static_cast<T>(inv[row]);
+    }
+}
+
+}  // namespace
+
+void ensure_ic0_schedule(Context& c) {
+    if (c.sweep_pattern_version == c.pattern_version) return;
+    const int n = static_cast<int>(c.n);
+    std::vector<int> rowptr(static_cast<size_t>(n) + 1), col(static_cast<size_t>(c.nnz)), diag(static_cast<size_t>(n));
+    LF_CUDA(cudaMemcpyAsync(rowptr.data(), c.rowptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, c.stream));
+    LF_CUDA(cudaMemcpyAsync(col.data(), c.col.p, sizeof(int) * c.nnz, cudaMemcpyDeviceToHost, c.stream));
+    LF_CUDA(cudaMemcpyAsync(diag.data(), c.diag.p, sizeof(int) * n, cudaMemcpyDeviceToHost, c.stream));
+    LF_CUDA(cudaStreamSynchronize(c.stream));
+    SweepSchedule fw, bw;
+    std::thread other([&] { sweep_schedule(n, rowptr.data(), col.data(), diag.data(), false, bw); });
+    sweep_schedule(n, rowptr.data(), col.data(), diag.data(), true, fw);
+    other.join();
+    // The forward sweep writes y(r) where the backward sweep reads it: r's backward position.
+    for (int p = 0; p < n; ++p) fw.desc[4 * static_cast<size_t>(p) + 3] = bw.position[static_cast<size_t>(fw.desc[4 * static_cast<size_t>(p)])];
+    const SweepSchedule* both[2] = {&fw, &bw};
+    long long need = 0;
+    c.sweep_max_width = 0;
+    c.sweep_max_distance = 0;
+    for (int d = 0; d < 2; ++d) {
+        const SweepSchedule& s = *both[d];
+        // Slots a level overwrites must hold no row a CTA still reads; CTAs run at
+        // most one level apart, so the ring spans the longest dependency distance
+        // plus two levels.
+        need = std::max(need, s.max_distance + 2LL * s.max_width);
+        c.sweep_max_width = std::max<i64>(c.sweep_max_width, s.max_width);
+        c.sweep_max_distance = std::max<i64>(c.sweep_max_distance, s.max_distance);
+        Context::Sweep& dst = c.sweep[d];
+        dst.levels = s.levels;
+        dst.entries = static_cast<int>(s.dep.size());
+        dst.level_begin.ensure(s.level_begin.size());
+        dst.desc.ensure(static_cast<size_t>(n));
+        dst.dep.ensure(std::max<size_t>(1, s.dep.size()));
+        LF_CUDA(cudaMemcpyAsync(dst.level_begin.p, s.level_begin.data(), sizeof(int) * s.level_begin.size(),
+                                cudaMemcpyHostToDevice, c.stream));
+        LF_CUDA(cudaMemcpyAsync(dst.desc.p, s.desc.data(), sizeof(int) * s.desc.size(), cudaMemcpyHostToDevice,
+                                c.stream));
+        if (!s.dep.empty())
+            LF_CUDA(cudaMemcpyAsync(dst.dep.p, s.dep.data(), sizeof(int) * s.dep.size(), cudaMemcpyHostToDevice,
+                                    c.stream));
+        dst.val_version = dst.val32_version = ~0ull;
+    }
+    int window = 256;
+    while (window < need && window <= kSweepRingMax) window *= 2;
+    c.sweep_window = window <= kSweepRingMax ? window : 0;
+    LF_CUDA(cudaStreamSynchronize(c.stream));  // the host schedules are released on return
+    c.sweep_pattern_version = c.pattern_version;
+}
+
+void ensure_ic0_sweep_values(Context& c, bool fp32) {
+    const int n = static_cast<int>(c.n);
+    const int grid = grid_for(n, kThreads, 16 * c.num_sms);
+    for (int d = 0; d < 2; ++d) {
+        Context::Sweep& s = c.sweep[d];
+        const int total = s.entries;
+        if (s.val_version != c.ic0_version) {
+            s.val.ensure(std::max(1, total));
+            s.inv.ensure(n);
+            ic0_schedule_values_kernel<double><<<grid, kThreads, 0, c.stream>>>(
+                n, d == 0, s.desc, c.rowptr, c.diag, c.ic0_val, c.ic0_inv, s.val, s.inv);
+            c.launches += 1;
+            s.val_version = c.ic0_version;
+        }
+        if (fp32 && s.val32_version != c.ic0_version) {
+            s.val32.ensure(std::max(1, total));
+            s.inv32.ensure(n);
+            ic0_schedule_values_kernel<float><<<grid, kThreads, 0, c.stream>>>(
+                n, d == 0, s.desc, c.rowptr, c.diag, c.ic0_val, c.ic0_inv, s.val32, s.inv32);
+            c.launches += 1;
+            s.val32_version = c.ic0_version;
+        }
+    }
+    LF_CUDA(cudaGetLastError());
+}
+
+bool ic0_use_levels(Context& c, bool required) {
+    if (c.ic0_sweep == LFGPU_IC0_SWEEP_POLLED && !required) return false;
+    LF_REQUIRE(c.ic0_sweep != LFGPU_IC0_SWEEP_POLLED, LFGPU_ERR_UNSUPPORTED,
+               "mixed-precision ic0 needs the level-scheduled sweeps");
+    ensure_ic0_schedule(c);
+    if (c.sweep_window > 0) return true;
+    LF_REQUIRE(!required && c.ic0_sweep == LFGPU_IC0_SWEEP_AUTO, LFGPU_ERR_UNSUPPORTED,
+               "the ic0 level schedule does not fit the sweep's shared-memory ring");
+    return false;
 }
 
 }  // namespace lfgpu

@@ -68,6 +68,23 @@ enum Ic0Slot {
     kIc0Slots = 8
 };
 void ensure_ic0(Context& c);
+// Level schedules of the two IC(0) sweeps, per pattern version (host schedule,
+// uploaded); sets c.sweep_window (0 when the ring cannot hold the schedule).
+void ensure_ic0_schedule(Context& c);
+// The factor in schedule order for the level sweeps, per K version: FP64, and the
+// FP32 copy when fp32 is set.  Requires ensure_ic0 and ensure_ic0_schedule.
+void ensure_ic0_sweep_values(Context& c, bool fp32);
+// Whether the level-scheduled sweeps run for this handle (option and schedule fit);
+// throws LFGPU_ERR_UNSUPPORTED when they are required but the schedule does not fit.
+bool ic0_use_levels(Context& c, bool required);
+
+// The level-scheduled sweeps run as one cluster of kSweepCluster CTAs of
+// kSweepThreads threads; every CTA keeps a ring of the last sweep_window results
+// in shared memory (kSweepStages mbarriers track the levels in flight).
+constexpr int kSweepCluster = 8;
+constexpr int kSweepThreads = 128;
+constexpr int kSweepStages = 4;
+constexpr int kSweepRingMax = 16384;
 
 // pattern.cu: CSR pattern and element->value map on the device; false if a node
 // has more elements than the device build handles (the caller builds on the host)

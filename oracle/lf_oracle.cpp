@@ -669,8 +669,13 @@ i64 lfo_element_colors(i64 n_nodes, i64 n_elem, const i64* nodes, i64* colors) {
 // strategy: natural order; colouring: colour groups in turn), src/solver.cpp:135-179
 // with the per-element matrices of src/solver.cpp:244-270.  Returns -1 - e for a
 // non-positive Jacobian in element e.
+// With colour groups (color_ptr[n_colors + 1] offsets into `order`, elements of one
+// colour sharing no node) each colour's scatter is a parallel loop, as
+// coloring_assembly runs it (src/solver.cpp:163-179); every value still receives
+// its terms in colour order, so the result equals the serial scatter bit for bit.
 i64 lfo_assemble(const double* xy, i64 n_elem, const i64* nodes, const double* young, const double* poisson,
-                 const double* thick, int plane_strain, const i64* map, const i64* order, double* values) {
+                 const double* thick, int plane_strain, const i64* map, const i64* order, double* values,
+                 const i64* color_ptr, i64 n_colors) {
     std::vector<double> ke(static_cast<size_t>(n_elem) * 64);
     i64 bad = 0;
 #pragma omp parallel for schedule(static)
@@ -686,6 +691,16 @@ i64 lfo_assemble(const double* xy, i64 n_elem, const i64* nodes, const double* y
         }
     }
     if (bad != 0) return bad;
+    if (order && color_ptr && n_colors > 0) {
+        for (i64 c = 0; c < n_colors; ++c) {
+#pragma omp parallel for schedule(static)
+            for (i64 k = color_ptr[c]; k < color_ptr[c + 1]; ++k) {
+                const i64 e = order[k];
+                for (int j = 0; j < 64; ++j) values[map[e * 64 + j]] += ke[static_cast<size_t>(e) * 64 + j];
+            }
+        }
+        return 0;
+    }
     for (i64 k = 0; k < n_elem; ++k) {
         const i64 e = order ? order[k] : k;
         for (int j = 0; j < 64; ++j) values[map[e * 64 + j]] += ke[static_cast<size_t>(e) * 64 + j];

@@ -42,7 +42,7 @@ def lib() -> ctypes.CDLL:
             "lfo_pattern_copy": (None, [vp, vp, vp, vp]),
             "lfo_pattern_free": (None, [vp]),
             "lfo_element_colors": (i64, [i64, i64, vp, vp]),
-            "lfo_assemble": (i64, [vp, i64, vp, vp, vp, vp, i32, vp, vp, vp]),
+            "lfo_assemble": (i64, [vp, i64, vp, vp, vp, vp, i32, vp, vp, vp, vp, i64]),
             "lfo_element_loads": (i32, [vp, vp, vp, i64, vp, vp, vp, i64, vp, vp, vp, vp, vp, vp]),
             "lfo_apply_dirichlet": (i64, [i64, vp, vp, vp, vp, i64, vp, vp]),
             "lfo_spmv_csr": (None, [i64, vp, vp, vp, vp, vp]),
@@ -230,15 +230,19 @@ def solve_model(model, *, storage=None, preconditioner=None, assembly=None, spli
     mi = model.material_index(model.element_material)
     young_e, nu_e, t_e = model.young[mi], model.poisson[mi], model.thickness[mi]
     order = None
+    color_ptr = None
     if assembly == "coloring":
         order = np.argsort(cl, kind="stable").astype(np.int64)
+        color_ptr = np.concatenate([[0], np.cumsum(np.bincount(cl))]).astype(np.int64)
     K = np.zeros(col.shape[0])
     t = time.perf_counter()
     rc = lib().lfo_assemble(_p(_c(model.xy)), en.shape[0], _p(_c(en, np.int64)), _p(_c(young_e)), _p(_c(nu_e)),
-                            _p(_c(t_e)), int(s.plane_mode), _p(_c(mp, np.int64)), _p(order), _p(K))
+                            _p(_c(t_e)), int(s.plane_mode), _p(_c(mp, np.int64)), _p(order), _p(K),
+                            _p(color_ptr), 0 if color_ptr is None else color_ptr.shape[0] - 1)
     if rc != 0:
         raise RuntimeError("Q4 stiffness evaluation received a non-positive Jacobian")
     out["timing"]["assembly_ms"] = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
     f = model.nodal_load_vector()
     be = model.element_index(model.body_element) if model.body_element.size else np.zeros(0, np.int64)
     ee = model.element_index(model.edge_element) if model.edge_element.size else np.zeros(0, np.int64)
@@ -249,6 +253,7 @@ def solve_model(model, *, storage=None, preconditioner=None, assembly=None, spli
                                  _p(_c(model.edge_second)), _p(f))
     if rc != 0:
         raise RuntimeError("element load evaluation failed")
+    out["timing"]["loads_ms"] = (time.perf_counter() - t) * 1e3
     out.update(K=K.copy(), f=f.copy())
     if stop_after == "assembly":
         return out

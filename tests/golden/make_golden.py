@@ -21,11 +21,16 @@ Cases:
   failures   degenerate inputs (NaN/inf/negative moduli, NaN/inf loads, a floating
              node): how the public solve() ends for each preconditioner and storage;
              a clockwise element and zero-length loaded edges: how the assembly ends
-  cfg1       the 200x200 workload: iteration counts, residuals, sampled u and R
-  cfg2       the 1000x1000 workload: known answers from the reference.  These runs
-             take hours; `--run-cfg2 DIR` makes them (ref_dump output per variant
-             in DIR/cfg2_<variant>) and `--cfg2-dir DIR` reads them back.  Without
-             either, the cfg2 entries already in golden.json and cfg2.npz are kept.
+  cfg1       the 200x200 workload: iteration counts, residuals, full u and R of the
+             Jacobi and IC(0) runs, every 101st DOF of the others
+  cfg2       the 1000x1000 workload: known answers from the reference (reports,
+             norms, max |u| and its DOF, every 2003rd u, u and R at 4000 seeded
+             DOFs).  These runs take about half an hour on 8 cores; `--run-cfg2 DIR`
+             makes them (ref_dump output per variant in DIR/cfg2_<variant>) and
+             `--cfg2-dir DIR` reads them back.  Without either, the cfg2 entries
+             already in golden.json and cfg2.npz are kept.
+
+`--only cfg1,cfg2` remakes only the named sections and keeps the other fixtures.
 
 Solve runs also carry the reference's post-processing (element centre and Gauss
 point fields, smoothed nodal stress); the small cases keep them.
@@ -179,7 +184,15 @@ def main() -> None:
     ap.add_argument("--run-cfg2", help="make the 1000x1000 reference runs in this directory (hours)")
     ap.add_argument("--failures-only", action="store_true",
                     help="remake only the failure-detection outcomes; keep every other fixture")
+    ap.add_argument("--only", default="",
+                    help="comma-separated sections to remake (single_q4, scrambled, grid6, beam, strain, adjoint, "
+                         "failures, cfg1, cfg2); the others keep their fixtures")
     args = ap.parse_args()
+    only = {x for x in args.only.split(",") if x}
+
+    def want(section: str) -> bool:
+        return not only or section in only
+
     if not os.path.exists(REF_DUMP):
         raise SystemExit("build the reference first: make -C oracle ref")
     if args.failures_only:
@@ -191,9 +204,14 @@ def main() -> None:
             json.dump(golden, fh, indent=1, sort_keys=True)
         return
     golden: dict = {}
+    if only and os.path.exists(os.path.join(OUT, "golden.json")):
+        with open(os.path.join(OUT, "golden.json")) as fh:
+            golden = json.load(fh)
 
     # --- single Q4 and scrambled mesh: every stage, serial and colouring assembly
     for name, model in (("single_q4", single_q4()), ("scrambled", scrambled())):
+        if not want(name):
+            continue
         arrays, report = run(model, "pattern=1", "ke=4", "precond=1", "subdomain_split=chunk",
                              "subdomain_nodes=1", "solve=1")
         col_arrays, col_report = run(model, "pattern=1", "assembly=coloring", "solve=1")
@@ -210,7 +228,27 @@ def main() -> None:
         save(name, arrays)
         golden[name] = report
 
-    # --- grid6: all iterative variants of tests/test_solver.cpp:398-448
+    if want("grid6"):
+        grid6_fixtures(golden)
+    if want("beam"):
+        beam_fixtures(golden)
+    if want("strain"):
+        strain_fixtures(golden)
+    if want("adjoint"):
+        adjoint_fixtures(golden)
+    if want("failures"):
+        golden["failures"], arrays = failure_outcomes()
+        save("failures", arrays)
+    if want("cfg1"):
+        cfg1_fixtures(golden)
+    if want("cfg2"):
+        cfg2_fixtures(golden, args)
+    with open(os.path.join(OUT, "golden.json"), "w") as fh:
+        json.dump(golden, fh, indent=1, sort_keys=True)
+
+
+def grid6_fixtures(golden: dict) -> None:
+    """All iterative variants of tests/test_solver.cpp:398-448."""
     model = grid6()
     arrays, report = run(model, "pattern=1", "ke=2", "precond=1", "subdomain_split=rcb", "subdomain_nodes=2")
     golden["grid6"] = {"pattern": report}
@@ -228,7 +266,9 @@ def main() -> None:
         golden["grid6"][vname] = vr
     save("grid6", arrays)
 
-    # --- perturbed two-material beam with gravity and pressure
+
+def beam_fixtures(golden: dict) -> None:
+    """Perturbed two-material beam with gravity and pressure."""
     model = mesh.perturbed_beam(24, 12, seed=7, settings=SolverSettings(
         tolerance=1e-10, max_iterations=20000, assembly="coloring"))
     arrays, report = run(model, "pattern=1", "ke=4", "precond=1", "subdomain_split=chunk", "subdomain_nodes=1")
@@ -243,7 +283,9 @@ def main() -> None:
         golden["beam"][vname] = vr
     save("beam", arrays)
 
-    # --- plane strain + RCM
+
+def strain_fixtures(golden: dict) -> None:
+    """Plane strain + RCM."""
     model = mesh.cantilever(16, 8, young=70e9, poisson=0.33, plane_mode=PLANE_STRAIN,
                             settings=SolverSettings(tolerance=1e-10, max_iterations=20000, assembly="coloring",
                                                     reordering="rcm"))
@@ -259,7 +301,9 @@ def main() -> None:
         golden["strain"][vname] = vr
     save("strain", arrays)
 
-    # --- adjoint: log-normal moduli, compliance and tip uy by central differences
+
+def adjoint_fixtures(golden: dict) -> None:
+    """Log-normal moduli, compliance and tip uy by central differences."""
     n = 20
     model = mesh.cantilever(n, n, poisson=0.3, per_element_young=mesh.lognormal_moduli(n * n, seed=11),
                             settings=SolverSettings(tolerance=1e-13, max_iterations=50000))
@@ -272,11 +316,20 @@ def main() -> None:
     golden["adjoint"] = report
     save("adjoint", arrays)
 
-    # --- failure detection: how the public solve() ends on degenerate inputs
-    golden["failures"], arrays = failure_outcomes()
-    save("failures", arrays)
 
-    # --- the 200x200 workload: iteration counts and sampled fields
+# Full u and R of the 200x200 workload are kept for these variants (80,802 values
+# each); the others keep every 101st DOF.
+CFG1_FULL = ("csr_jacobi", "csr_ic0")
+# DOFs of the 1000x1000 runs whose u and R are kept: seeded, sorted.
+CFG2_SAMPLE = 4000
+
+
+def cfg2_sample_dofs(n: int) -> np.ndarray:
+    return np.sort(np.random.default_rng(20261204).choice(n, size=CFG2_SAMPLE, replace=False))
+
+
+def cfg1_fixtures(golden: dict) -> None:
+    """The 200x200 workload: iteration counts and fields."""
     model = mesh.workload(1)
     arrays, report = run(model, "pattern=1")
     keep = {"rowptr_sum": np.array([arrays["rowptr"].sum()]), "col_sum": np.array([arrays["col"].sum()]),
@@ -285,6 +338,9 @@ def main() -> None:
     golden["cfg1"] = {"pattern": report, "nnz": int(arrays["col"].shape[0])}
     for vname in ("csr_jacobi", "bsr_jacobi", "csr_ic0", "bsr_block1", "bsr_block64"):
         va, vr = run(model, "solve=1", *VARIANTS[vname])
+        if vname in CFG1_FULL:
+            keep[f"u_{vname}_full"] = va["u"]
+            keep[f"R_{vname}_full"] = va["R"]
         keep[f"u_{vname}"] = va["u"][::101]
         keep[f"R_{vname}"] = va["R"][::101]
         vr["u_norm"] = float(np.linalg.norm(va["u"]))
@@ -292,7 +348,10 @@ def main() -> None:
         golden["cfg1"][vname] = vr
     save("cfg1", keep)
 
-    # --- the 1000x1000 workload (long runs, made separately)
+
+def cfg2_fixtures(golden: dict, args) -> None:
+    """The 1000x1000 workload (long runs, made separately): the reports, u at every
+    2003rd DOF, and u and R at CFG2_SAMPLE seeded DOFs with max |u| and its DOF."""
     cfg2 = {}
     keep = {}
     big = args.cfg2_dir or args.run_cfg2
@@ -314,8 +373,14 @@ def main() -> None:
             rep["u_norm"] = float(np.linalg.norm(u))
             rep["R_norm"] = float(np.linalg.norm(r))
             rep["R_y_sum"] = float(r[1::2].sum())
+            rep["u_absmax"] = float(np.abs(u).max())
+            rep["u_absmax_dof"] = int(np.abs(u).argmax())
             cfg2[vname] = rep
             keep[f"u_{vname}"] = u[::2003]
+            dofs = cfg2_sample_dofs(u.shape[0])
+            keep["sample_dofs"] = dofs
+            keep[f"u_{vname}_sample"] = u[dofs]
+            keep[f"R_{vname}_sample"] = r[dofs]
     if cfg2:
         golden["cfg2"] = cfg2
         save("cfg2", keep)
@@ -324,9 +389,6 @@ def main() -> None:
             old = json.load(fh)
         if "cfg2" in old:
             golden["cfg2"] = old["cfg2"]
-
-    with open(os.path.join(OUT, "golden.json"), "w") as fh:
-        json.dump(golden, fh, indent=1, sort_keys=True)
 
 
 if __name__ == "__main__":
