@@ -605,7 +605,7 @@ def run_ours(args) -> int:
     # other variants, one solve each (device time of the solve alone)
     variants = []
     ctx.set_subdomains(64, "rcb")  # the reference's default block setting, for the "subdomain" variant
-    for prec, st, pc, pers in (("mixed", "bsr", "block", False), ("mixed", "csr", "jacobi", False),
+    for prec, st, pc, pers in () if args.no_variants else (("mixed", "bsr", "block", False), ("mixed", "csr", "jacobi", False),
                                ("fp64", "csr", "jacobi", False), ("fp64", "bsr", "block", False),
                                ("mixed", "bsr", "subdomain", False),
                                ("mixed", "csr", "ic0", False), ("mixed", "bsr", "ic0", False),
@@ -760,6 +760,7 @@ def main() -> int:
                     help="loop passes launched on the stream to time the inner product per launch")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-beam", action="store_true", help="skip the 2000x1000 beam measurement")
+    ap.add_argument("--no-variants", action="store_true", help="skip the other storage/preconditioner variants")
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling run for ncu: one step capped at this many PCG iterations (not a benchmark)")
     args = ap.parse_args()

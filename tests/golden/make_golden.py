@@ -24,8 +24,8 @@ Cases:
   cfg1       the 200x200 workload: iteration counts, residuals, full u and R of the
              Jacobi and IC(0) runs, every 101st DOF of the others
   cfg2       the 1000x1000 workload: known answers from the reference (reports,
-             norms, max |u| and its DOF, every 2003rd u, u and R at 4000 seeded
-             DOFs).  These runs take about half an hour on 8 cores; `--run-cfg2 DIR`
+             norms, max |u| and its DOF, every 2003rd u, u at 4000 seeded DOFs, R at
+             every constrained DOF).  These runs take about half an hour on 8 cores; `--run-cfg2 DIR`
              makes them (ref_dump output per variant in DIR/cfg2_<variant>) and
              `--cfg2-dir DIR` reads them back.  Without either, the cfg2 entries
              already in golden.json and cfg2.npz are kept.
@@ -328,6 +328,13 @@ def cfg2_sample_dofs(n: int) -> np.ndarray:
     return np.sort(np.random.default_rng(20261204).choice(n, size=CFG2_SAMPLE, replace=False))
 
 
+def cfg2_fixed_dofs() -> np.ndarray:
+    """The constrained DOFs of the 1000x1000 workload, in node-ID order."""
+    m = mesh.workload(2)
+    m.sort_and_index()
+    return np.sort(m.constraints()[0]).astype(np.int64)
+
+
 def cfg1_fixtures(golden: dict) -> None:
     """The 200x200 workload: iteration counts and fields."""
     model = mesh.workload(1)
@@ -380,7 +387,10 @@ def cfg2_fixtures(golden: dict, args) -> None:
             dofs = cfg2_sample_dofs(u.shape[0])
             keep["sample_dofs"] = dofs
             keep[f"u_{vname}_sample"] = u[dofs]
-            keep[f"R_{vname}_sample"] = r[dofs]
+            # The reactions that carry load: every constrained DOF (the clamped edge).
+            fixed = cfg2_fixed_dofs()
+            keep["fixed_dofs"] = fixed
+            keep[f"R_{vname}_fixed"] = r[fixed]
     if cfg2:
         golden["cfg2"] = cfg2
         save("cfg2", keep)
