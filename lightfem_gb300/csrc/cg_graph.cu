@@ -97,6 +97,7 @@ struct CgArgs {
     // IC(0) level-scheduled sweeps (ic0.cu builds the schedules): [0] forward, [1] backward
     struct SweepPlan {
         const int* level_begin;    // 2 per level + 2: first position, first entry
+        const int4* pieces;        // per level and CTA: first and end position, first and end entry
         const int4* desc;          // per position: row, first entry, end entry, output index
         const int* dep;            // per entry: position of the row it depends on
         const void* val;           // factor entries in schedule order (double or float)
@@ -104,7 +105,10 @@ struct CgArgs {
         int levels;
     } sw[2];
     int sw_window;                 // ring slots per CTA (a power of two)
+    int sw_maxp, sw_maxe;          // the largest piece: positions, entries (the stage size)
     void* sw_y;                    // forward result in backward positions (double or float)
+    void* sw_rhs;                  // r in forward positions (double or float)
+    float* sw_rr;                  // mixed: r32 in backward positions (the backward sweep's r.z)
     int blocks;
     CgState* st;
     DeviceStatus* status;
@@ -319,13 +323,8 @@ __device__ __forceinline__ void bsr64_rows(const CgArgs& a, const G& g, Out&& ou
 // interior node's row cost one round of gather latency instead of three.  The
 // grid-stride loop loads the next row's block offsets while this row's blocks
 // stream, which takes one dependent load off each row's chain.
-//
-// Lanes 0 and 1 of each quad own DOFs 2 node and 2 node + 1 of the block row: each
-// loads its DOF's operands own(dof) before the row's blocks, so those loads overlap
-// the block stream instead of following it, and out(dof, row sum, operands) runs
-// on that lane.
-template <typename Own, typename G, typename Out>
-__device__ __forceinline__ void bsr32_rows(const CgArgs& a, const Own& own, const G& g, Out&& out) {
+template <typename G, typename Out>
+__device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& out) {
     const int lane = threadIdx.x & 31, sub = lane & 3;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int stride = ((gridDim.x * blockDim.x) >> 5) * 8;
@@ -342,10 +341,6 @@ __device__ __forceinline__ void bsr32_rows(const CgArgs& a, const Own& own, cons
             nb_b = __ldg(a.brow + node + stride);
             nb_e = __ldg(a.brow + node + stride + 1);
         }
-        const int dof = 2 * node + (sub & 1);
-        const bool owner = act && sub < 2;
-        decltype(own(0)) mine{};
-        if (owner) mine = own(dof);
         float s0 = 0.f, s1 = 0.f;
         if (act) {
             // Columns as 16-bit offsets from the block row when they fit (half the bytes).
@@ -370,7 +365,7 @@ __device__ __forceinline__ void bsr32_rows(const CgArgs& a, const Own& own, cons
         }
         s0 = quad_sum(s0);
         s1 = quad_sum(s1);
-        if (owner) out(dof, sub ? s1 : s0, mine);
+        if (act && sub == 0) out(node, make_float2(s0, s1));
     }
 }
 
@@ -654,17 +649,9 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
     });
 }
 
-// The operands a product lane loads for its own DOF ahead of the row's blocks.
-struct DofOperands {
-    float2 zp;  // (z, p_old)
-    float hi, lo;
-};
-
 // q = K32 p with p = z + beta p_old formed on the fly; each row writes its p.
-// Eight CTAs per SM (32 registers a thread): the kernel is bound by load latency,
-// so every resident warp counts.
 template <int STORAGE>
-__global__ void __launch_bounds__(kThreads, 8) mx_product(CgArgs a) {
+__global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
     if (a.st->done) return;
     const float beta = a.st->beta32;
     const float4* zp4 = zp_buffer(a, a.st->it);
@@ -685,25 +672,21 @@ __global__ void __launch_bounds__(kThreads, 8) mx_product(CgArgs a) {
                        acc.add(pn * y);
                    });
     } else {
-        const float2* zp2 = reinterpret_cast<const float2*>(zp4);
+        const float2* hi2 = reinterpret_cast<const float2*>(a.dhi);
+        const float2* lo2 = reinterpret_cast<const float2*>(a.dlo);
         bsr32_rows(a,
-                   [&](int dof) {
-                       DofOperands o;
-                       o.zp = zp2[dof];
-                       o.hi = a.dhi[dof];
-                       o.lo = a.dlo[dof];
-                       return o;
-                   },
                    [&](int c) {
                        const float4 v = zp4[c];
                        return make_float2(pnew(v.x, v.y, beta), pnew(v.z, v.w, beta));
                    },
-                   [&](int dof, float off, const DofOperands& o) {
-                       const float pn = pnew(o.zp.x, o.zp.y, beta);
-                       const float y = with_diag(off, o.hi, o.lo, pn);
-                       a.p32[dof] = pn;
-                       a.q32[dof] = y;
-                       acc.add(pn * y);
+                   [&](int node, float2 off) {
+                       const float4 v = zp4[node];
+                       const float2 pn = make_float2(pnew(v.x, v.y, beta), pnew(v.z, v.w, beta));
+                       const float2 h = hi2[node], l = lo2[node];
+                       const float2 y = make_float2(with_diag(off.x, h.x, l.x, pn.x), with_diag(off.y, h.y, l.y, pn.y));
+                       reinterpret_cast<float2*>(a.p32)[node] = pn;
+                       reinterpret_cast<float2*>(a.q32)[node] = y;
+                       acc.add(pn.x * y.x + pn.y * y.y);
                    });
     }
     FloatPair v[1] = {acc};
@@ -974,29 +957,39 @@ __global__ void __launch_bounds__(kSweepRows) ic0_backward(CgArgs a) {
 // The same two sweeps, scheduled by levels instead of polls: a row's level is one
 // more than the deepest row it depends on, so the rows of one level are
 // independent.  One cluster of kSweepCluster CTAs walks the levels in order; each
-// level's rows are split into one contiguous piece per CTA, one thread per row.
+// level's rows are split into one contiguous piece per CTA, one consumer thread
+// per row.
+//
+// Operands arrive by TMA.  The schedule stores each level's rows, entries,
+// pivots and right-hand sides contiguously, so a producer warp per CTA copies the
+// CTA's piece of a level (row descriptors, entry positions and values, reciprocal
+// pivots, right-hand sides) into one of kSweepStages shared-memory stages with
+// cp.async.bulk, up to kSweepStages levels ahead; the consumers find their
+// operands in shared memory when the level starts.
 //
 // Results travel through shared memory, not L2: every CTA keeps a ring of the last
-// sw_window results (slot = schedule position mod sw_window), and a thread that
+// sw_window results (slot = schedule position mod sw_window), and a consumer that
 // finishes a row stores its result into every CTA's ring with st.async, which
 // also counts the bytes on that CTA's mbarrier of the level.  A CTA starts level L
 // once its mbarrier of level L - 1 has seen the whole level (width x size bytes),
-// so no cluster-wide barrier runs per level and the loads for the next levels stay
-// in flight across the wait: each thread loads the next level's row (descriptor,
-// right-hand side, pivot, the first kSweepRegEntries entries) into registers while
-// the current level runs, and the descriptor two levels ahead.  CTAs run at most
-// one level apart, so the ring spans the longest dependency distance plus two
-// levels (ensure_ic0_schedule checks it), and kSweepStages mbarriers cycle over the
-// levels; the warps of a CTA meet once per level, after the wait.  Waits are
-// bounded: on expiry the kernel records LFGPU_ERR_TIMEOUT and ends the solve.
+// so no cluster-wide barrier runs per level.  CTAs run at most one level apart, so
+// the ring spans the longest dependency distance plus two levels
+// (ensure_ic0_schedule checks it), and kSweepRingBars mbarriers cycle over the
+// levels; the consumer warps of a CTA meet once per level.  Waits are bounded: on
+// expiry the kernel records LFGPU_ERR_TIMEOUT and ends the solve.
 //
 // The arithmetic of a row is the polled sweeps': terms subtracted in the
 // reference's order, products and differences rounded separately, so the FP64
 // sweeps equal the reference's application bit for bit.  MODE 0 / 1: FP64 forward
 // (r -> y in backward order) / backward (-> z); MODE 2 / 3: the mixed loop's FP32
 // forward (r32) / backward, which writes z into the (z, p) copy the next product
-// reads and reduces r.z (rho and beta, as the subdomain application does).
-constexpr int kSweepRegEntries = 10;  // entries of a row held in registers (an interior Q4 row has at most 9)
+// reads and reduces r.z (rho and beta, as the subdomain application does).  The
+// forward sweep reads r in schedule order (ic0_sweep_inputs gathers it first), the
+// backward sweep the forward result, which the forward sweep writes in backward
+// order.
+constexpr int kSweepRingBars = 4;
+constexpr int kSweepConsumers = kSweepThreads;   // one row per consumer thread and pass
+constexpr int kSweepBlock = kSweepThreads + 32;  // plus the producer warp
 
 __device__ __forceinline__ unsigned cluster_rank() {
     unsigned r;
@@ -1022,7 +1015,7 @@ __device__ __forceinline__ void store_remote(unsigned addr, float v, unsigned ba
                  "r"(bar)
                  : "memory");
 }
-__device__ __forceinline__ bool level_done(unsigned long long* bar, unsigned parity) {
+__device__ __forceinline__ bool phase_done(unsigned long long* bar, unsigned parity) {
     unsigned ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -1031,14 +1024,21 @@ __device__ __forceinline__ bool level_done(unsigned long long* bar, unsigned par
         : "memory");
     return ok != 0;
 }
-// Bounded wait for a level's results; false when it ran out (or another wait did).
-__device__ __forceinline__ bool wait_level(unsigned long long* bar, unsigned parity, DeviceStatus* status, int level) {
-    if (level_done(bar, parity)) return true;
+// Bounded wait for an mbarrier phase; false when it ran out (or another wait did).
+__device__ __forceinline__ bool wait_phase(unsigned long long* bar, unsigned parity, DeviceStatus* status, int level) {
+    if (phase_done(bar, parity)) return true;
     const unsigned long long t0 = global_ns();
     for (unsigned it = 1;; ++it) {
-        if (level_done(bar, parity)) return true;
+        if (phase_done(bar, parity)) return true;
         if ((it & 15u) == 0u && wait_expired(status, t0, level)) return false;
     }
+}
+__device__ __forceinline__ void arrive(unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// The consumer warps' own barrier (the producer warp does not take part).
+__device__ __forceinline__ void consumers_sync() {
+    asm volatile("bar.sync 1, %0;" ::"n"(kSweepConsumers) : "memory");
 }
 
 __device__ __forceinline__ double sweep_term(double acc, double l, double v) { return __dsub_rn(acc, __dmul_rn(l, v)); }
@@ -1063,158 +1063,163 @@ __device__ __forceinline__ void rho_from_application(const CgArgs& a, const doub
     set_loop(a, !st->done);
 }
 
-template <typename T>
-struct SweepRow {
-    int pos;   // schedule position, -1: none
-    int4 d;    // row, first entry, end entry, output index
-    T rhs, inv, r;
-    int dep[kSweepRegEntries];
-    T val[kSweepRegEntries];
-};
+// Elements of type E that a copy from the 16-byte boundary at or below index i
+// carries in front of element i (the array base is 16-byte aligned).
+template <typename E>
+__device__ __forceinline__ int lead_of(int i) {
+    return i & (16 / static_cast<int>(sizeof(E)) - 1);
+}
+
+// r gathered into the forward schedule's order (and, for the mixed backward
+// sweep's r.z, into the backward schedule's), before the forward sweep.
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads) ic0_sweep_inputs(CgArgs a) {
+    if (a.st->done) return;
+    const int4* __restrict__ fd = a.sw[0].desc;
+    const int4* __restrict__ bd = a.sw[1].desc;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+        if (MIXED) {
+            static_cast<float*>(a.sw_rhs)[p] = a.r32[fd[p].x];
+            a.sw_rr[p] = a.r32[bd[p].x];
+        } else {
+            static_cast<double*>(a.sw_rhs)[p] = a.r[fd[p].x];
+        }
+    }
+}
 
 template <int MODE>
-__global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepThreads) ic0_level_sweep(CgArgs a) {
+__global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBlock) ic0_level_sweep(CgArgs a) {
     using T = typename std::conditional<(MODE < 2), double, float>::type;
     constexpr bool kFwd = (MODE & 1) == 0;
-    constexpr bool kMixed = MODE >= 2;
     constexpr int S = kSweepStages;
-    constexpr int E = kSweepRegEntries;
+    constexpr int SR = kSweepRingBars;
     if (a.st->done) return;  // read before the kernel changes anything: the same in every CTA
-    extern __shared__ __align__(16) unsigned char sweep_smem[];
-    __shared__ __align__(8) unsigned long long bars[S];
+    extern __shared__ __align__(128) unsigned char sweep_smem[];
+    __shared__ __align__(8) unsigned long long full[S], empty[S], ringbar[SR];
+    __shared__ int4 piece_of[S];
     __shared__ int s_failed;
-    T* ring = reinterpret_cast<T*>(sweep_smem);
     const CgArgs::SweepPlan& sp = a.sw[kFwd ? 0 : 1];
-    const int* __restrict__ lvl = sp.level_begin;
-    const int4* __restrict__ desc = sp.desc;
-    const int* __restrict__ dep = sp.dep;
-    const T* __restrict__ val = static_cast<const T*>(sp.val);
-    const T* __restrict__ pinv = static_cast<const T*>(sp.inv);
-    T* yb = static_cast<T*>(a.sw_y);
     const int levels = sp.levels;
     const int mask = a.sw_window - 1;
     const unsigned rank = cluster_rank();
     const int tid = threadIdx.x;
-    auto width_bytes = [&](int L) { return static_cast<unsigned>(__ldg(lvl + 2 * L + 2) - __ldg(lvl + 2 * L)) * sizeof(T); };
+    T* ring = reinterpret_cast<T*>(sweep_smem);
+    unsigned char* stages = sweep_smem + sweep_round16(a.sw_window * static_cast<int>(sizeof(T)));
+    const SweepStageLayout lay = sweep_stage_layout(static_cast<int>(sizeof(T)), a.sw_maxp, a.sw_maxe);
+    auto width_bytes = [&](int L) {
+        return static_cast<unsigned>(__ldg(sp.level_begin + 2 * L + 2) - __ldg(sp.level_begin + 2 * L)) *
+               static_cast<unsigned>(sizeof(T));
+    };
     if (tid == 0) {
         s_failed = 0;
-        for (int s = 0; s < S; ++s) mbar_init(bars + s, 1);
+        for (int s = 0; s < S; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        for (int s = 0; s < SR; ++s) mbar_init(ringbar + s, 1);
         mbar_init_fence();
-        for (int L = 0; L < S && L < levels; ++L) mbar_expect_tx(bars + L, width_bytes(L));
+        for (int L = 0; L < SR && L < levels; ++L) mbar_expect_tx(ringbar + L, width_bytes(L));
     }
-    cluster_sync_all();  // every CTA's mbarriers are armed before any result arrives
-    unsigned ring_at[kSweepCluster], bar_at[kSweepCluster];
-#pragma unroll
-    for (int k = 0; k < kSweepCluster; ++k) {
-        ring_at[k] = cluster_address(smem_u32(ring), k);
-        bar_at[k] = cluster_address(smem_u32(bars), k);
-    }
-    // This thread's first position in level L and the end of this CTA's piece.
-    auto piece = [&](int L, int& p, int& end) {
-        const int p0 = __ldg(lvl + 2 * L), p1 = __ldg(lvl + 2 * L + 2);
-        const int chunk = (p1 - p0 + kSweepCluster - 1) / kSweepCluster;
-        const int first = p0 + static_cast<int>(rank) * chunk;
-        end = min(p1, first + chunk);
-        p = first + tid;
-    };
-    auto rhs_of = [&](int p, int row) -> T {
-        if constexpr (!kFwd) return yb[p];
-        else if constexpr (kMixed) return a.r32[row];
-        else return a.r[row];
-    };
-    auto load_row = [&](SweepRow<T>& w, int p, int4 d) {
-        w.pos = p;
-        w.d = d;
-        if (p < 0) return;
-        w.rhs = rhs_of(p, d.x);
-        w.inv = __ldg(pinv + p);
-        if constexpr (MODE == 3) w.r = a.r32[d.x];
-#pragma unroll
-        for (int k = 0; k < E; ++k) {
-            if (d.y + k < d.z) {
-                w.dep[k] = __ldg(dep + d.y + k);
-                w.val[k] = __ldg(val + d.y + k);
-            }
-        }
-    };
-    FloatPair rz;
-    auto finish_row = [&](int p, int4 d, T rhs, T inv, T r, const int* dk, const T* vk, int L) {
-        T acc = rhs;
-#pragma unroll
-        for (int k = 0; k < E; ++k)
-            if (d.y + k < d.z) acc = sweep_term(acc, vk[k], ring[dk[k] & mask]);
-        for (int j = d.y + E; j < d.z; ++j) acc = sweep_term(acc, __ldg(val + j), ring[__ldg(dep + j) & mask]);
-        const T y = sweep_scale(acc, inv);
-        const unsigned slot = static_cast<unsigned>(p & mask) * sizeof(T);
-        const unsigned bar = static_cast<unsigned>(L % S) * 8u;
-#pragma unroll
-        for (int k = 0; k < kSweepCluster; ++k) store_remote(ring_at[k] + slot, y, bar_at[k] + bar);
-        if constexpr (kFwd) {
-            yb[d.w] = y;
-        } else if constexpr (!kMixed) {
-            a.z[d.x] = y;
-        } else {
-            // z of DOF 2m sits in .x of node m's (z, p) float4, z of DOF 2m + 1 in .z.
-            reinterpret_cast<float*>(zp_buffer(a, a.st->it))[4 * (d.x >> 1) + 2 * (d.x & 1)] = y;
-            rz.add(r * y);
-        }
-    };
-    const int4 none = make_int4(0, 0, 0, 0);
-    SweepRow<T> cur, nxt;
-    int4 d1 = none, d2 = none;
-    int p1 = -1, p2 = -1;
-    {
-        int p, end;
-        piece(0, p, end);
-        load_row(cur, p < end ? p : -1, p < end ? __ldg(desc + p) : none);
-        if (levels > 1) {
-            piece(1, p, end);
-            p1 = p < end ? p : -1;
-            if (p1 >= 0) d1 = __ldg(desc + p1);
-        }
-    }
+    cluster_sync_all();  // every CTA's mbarriers are armed before any copy or result arrives
     bool ok = true;
-    for (int L = 0; L < levels; ++L) {
-        // Loads for the next levels, issued before this level's wait.
-        p2 = -1;
-        if (L + 2 < levels) {
-            int p, end;
-            piece(L + 2, p, end);
-            if (p < end) {
-                p2 = p;
-                d2 = __ldg(desc + p);
+    FloatPair rz;  // the mixed backward sweep's r.z (zero on the producer warp)
+    if (tid >= kSweepConsumers) {
+        // ---- producer warp: one lane copies each level's piece into its stage.
+        if (tid == kSweepConsumers) {
+            const unsigned long long policy = l2_evict_first_policy();
+            const T* rhs_src = static_cast<const T*>(kFwd ? a.sw_rhs : a.sw_y);
+            for (int L = 0; L < levels; ++L) {
+                const int s = L % S;
+                // The stage is free once the consumers are done with level L - S.
+                if (L >= S) ok = wait_phase(empty + s, static_cast<unsigned>(L / S - 1) & 1u, a.status, L) && ok;
+                const int4 pc = __ldg(sp.pieces + static_cast<size_t>(L) * kSweepCluster + rank);
+                piece_of[s] = pc;
+                unsigned char* st = stages + static_cast<size_t>(s) * lay.bytes;
+                const int cnt = pc.y - pc.x;
+                if (cnt <= 0) {
+                    mbar_expect_tx(full + s, 0u);  // an empty piece: the phase completes at once
+                    continue;
+                }
+                const int dep0 = pc.z - lead_of<int>(pc.z), val0 = pc.z - lead_of<T>(pc.z);
+                const int pos0 = pc.x - lead_of<T>(pc.x);
+                const bool entries = pc.w > pc.z;
+                const unsigned b_desc = static_cast<unsigned>(cnt) * 16u;
+                const unsigned b_dep = entries ? static_cast<unsigned>(sweep_round16((pc.w - dep0) * 4)) : 0u;
+                const unsigned b_val =
+                    entries ? static_cast<unsigned>(sweep_round16((pc.w - val0) * static_cast<int>(sizeof(T)))) : 0u;
+                const unsigned b_pos = static_cast<unsigned>(sweep_round16((pc.y - pos0) * static_cast<int>(sizeof(T))));
+                mbar_expect_tx(full + s, b_desc + b_dep + b_val + (MODE == 3 ? 3u : 2u) * b_pos);
+                bulk_copy(st + lay.desc, sp.desc + pc.x, b_desc, full + s, policy);
+                if (entries) {
+                    bulk_copy(st + lay.dep, sp.dep + dep0, b_dep, full + s, policy);
+                    bulk_copy(st + lay.val, static_cast<const T*>(sp.val) + val0, b_val, full + s, policy);
+                }
+                bulk_copy(st + lay.inv, static_cast<const T*>(sp.inv) + pos0, b_pos, full + s, policy);
+                bulk_copy(st + lay.rhs, rhs_src + pos0, b_pos, full + s, policy);
+                if (MODE == 3) bulk_copy(st + lay.rr, a.sw_rr + pos0, b_pos, full + s, policy);
             }
         }
-        if (L + 1 < levels) load_row(nxt, p1, d1);
-        if (L > 0) {
-            const int prev = L - 1;
-            ok = wait_level(bars + prev % S, static_cast<unsigned>(prev / S) & 1u, a.status, prev) && ok;
-            // Every thread of the CTA has seen level prev complete: its mbarrier is
-            // free again, armed for level prev + S.  (This also keeps the CTA's warps
-            // on one level, so no thread polls a phase that has moved on.)
-            __syncthreads();
-            if (tid == 0 && prev + S < levels) mbar_expect_tx(bars + prev % S, width_bytes(prev + S));
+    } else {
+        // ---- consumers: one row per thread and pass.
+        unsigned ring_at[kSweepCluster], bar_at[kSweepCluster];
+#pragma unroll
+        for (int k = 0; k < kSweepCluster; ++k) {
+            ring_at[k] = cluster_address(smem_u32(ring), k);
+            bar_at[k] = cluster_address(smem_u32(ringbar), k);
         }
-        if (cur.pos >= 0) finish_row(cur.pos, cur.d, cur.rhs, cur.inv, cur.r, cur.dep, cur.val, L);
-        // Levels wider than the cluster's threads: further rows, loaded here.
-        {
-            int p, end;
-            piece(L, p, end);
-            for (p += kSweepThreads; p < end; p += kSweepThreads) {
-                SweepRow<T> w;
-                load_row(w, p, __ldg(desc + p));
-                finish_row(w.pos, w.d, w.rhs, w.inv, w.r, w.dep, w.val, L);
+        for (int L = 0; L < levels; ++L) {
+            const int s = L % S;
+            // Bytes the ring mbarrier of level L - 1 expects when it is armed again,
+            // for level L - 1 + SR, at the end of this level: loaded now, used then.
+            const bool rearm = tid == 0 && L > 0 && L - 1 + SR < levels;
+            const unsigned rearm_bytes = rearm ? width_bytes(L - 1 + SR) : 0u;
+            ok = wait_phase(full + s, static_cast<unsigned>(L / S) & 1u, a.status, L) && ok;
+            if (L > 0) {
+                const int prev = L - 1;
+                ok = wait_phase(ringbar + prev % SR, static_cast<unsigned>(prev / SR) & 1u, a.status, prev) && ok;
+            }
+            const int4 pc = piece_of[s];
+            const unsigned char* st = stages + static_cast<size_t>(s) * lay.bytes;
+            const int4* sdesc = reinterpret_cast<const int4*>(st + lay.desc);
+            const int dep0 = pc.z - lead_of<int>(pc.z), val0 = pc.z - lead_of<T>(pc.z);
+            const int pos0 = pc.x - lead_of<T>(pc.x);
+            const int* sdep = reinterpret_cast<const int*>(st + lay.dep);  // entry j at [j - dep0]
+            const T* sval = reinterpret_cast<const T*>(st + lay.val);      // entry j at [j - val0]
+            const T* sinv = reinterpret_cast<const T*>(st + lay.inv);      // position p at [p - pos0]
+            const T* srhs = reinterpret_cast<const T*>(st + lay.rhs);
+            const T* srr = reinterpret_cast<const T*>(st + lay.rr);
+            const unsigned bar_off = static_cast<unsigned>(L % SR) * 8u;
+            for (int t = tid; t < pc.y - pc.x; t += kSweepConsumers) {
+                const int p = pc.x + t;
+                const int4 d = sdesc[t];
+                T acc = srhs[p - pos0];
+                for (int j = d.y; j < d.z; ++j) acc = sweep_term(acc, sval[j - val0], ring[sdep[j - dep0] & mask]);
+                const T y = sweep_scale(acc, sinv[p - pos0]);
+                const unsigned slot = static_cast<unsigned>(p & mask) * static_cast<unsigned>(sizeof(T));
+#pragma unroll
+                for (int k = 0; k < kSweepCluster; ++k) store_remote(ring_at[k] + slot, y, bar_at[k] + bar_off);
+                if constexpr (kFwd) {
+                    static_cast<T*>(a.sw_y)[d.w] = y;
+                } else if constexpr (MODE == 1) {
+                    a.z[d.x] = y;
+                } else {
+                    // z of DOF 2m sits in .x of node m's (z, p) float4, z of DOF 2m + 1 in .z.
+                    reinterpret_cast<float*>(zp_buffer(a, a.st->it))[4 * (d.x >> 1) + 2 * (d.x & 1)] = y;
+                    rz.add(srr[p - pos0] * y);
+                }
+            }
+            consumers_sync();  // every consumer is done with stage s and has seen level L - 1 arrive
+            if (tid == 0) {
+                arrive(empty + s);
+                if (rearm) mbar_expect_tx(ringbar + (L - 1) % SR, rearm_bytes);
             }
         }
-        cur = nxt;
-        if (L + 1 >= levels) cur.pos = -1;
-        p1 = p2;
-        d1 = d2;
+        // Every result bound for this CTA has arrived before it exits.
+        if (levels > 0)
+            ok = wait_phase(ringbar + (levels - 1) % SR, static_cast<unsigned>((levels - 1) / SR) & 1u, a.status,
+                            levels - 1) &&
+                 ok;
     }
-    // Every result bound for this CTA has arrived before it exits.
-    if (levels > 0)
-        ok = wait_level(bars + (levels - 1) % S, static_cast<unsigned>((levels - 1) / S) & 1u, a.status, levels - 1) &&
-             ok;
     if (!ok) s_failed = 1;
     __syncthreads();
     if (s_failed) {
@@ -1503,8 +1508,10 @@ cudaGraphNode_t add_mixed_apply(cudaGraph_t g, cudaGraphNode_t dep, CgArgs* a, i
         add_kernel(g, &n1, &dep, 1, mx_sub_apply, sub_grid, a, 0, sub_threads);
         return n1;
     } else {
-        add_kernel(g, &n1, &dep, 1, ic0_level_sweep<2>, kSweepCluster, a, smem, kSweepThreads);
-        add_kernel(g, &n2, &n1, 1, ic0_level_sweep<3>, kSweepCluster, a, smem, kSweepThreads);
+        cudaGraphNode_t n0;
+        add_kernel(g, &n0, &dep, 1, ic0_sweep_inputs<true>, a->blocks, a);
+        add_kernel(g, &n1, &n0, 1, ic0_level_sweep<2>, kSweepCluster, a, smem, kSweepBlock);
+        add_kernel(g, &n2, &n1, 1, ic0_level_sweep<3>, kSweepCluster, a, smem, kSweepBlock);
         return n2;
     }
 }
@@ -1594,10 +1601,12 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
     };
     auto sub_apply = [&](int phase) {
         if constexpr (PRECOND == LFGPU_PRECOND_IC0) {
-            ic0_level_sweep<2><<<kSweepCluster, kSweepThreads, smem, stream>>>(*a);
+            ic0_sweep_inputs<true><<<a->blocks, kThreads, 0, stream>>>(*a);
+            LF_CUDA(cudaGetLastError());
+            ic0_level_sweep<2><<<kSweepCluster, kSweepBlock, smem, stream>>>(*a);
             LF_CUDA(cudaGetLastError());
             trail.mark(phase);
-            ic0_level_sweep<3><<<kSweepCluster, kSweepThreads, smem, stream>>>(*a);
+            ic0_level_sweep<3><<<kSweepCluster, kSweepBlock, smem, stream>>>(*a);
         } else {
             mx_sub_apply<<<sub_grid, sub_threads, 0, stream>>>(*a);
         }
@@ -1646,8 +1655,10 @@ cudaGraphNode_t add_apply(cudaGraph_t g, cudaGraphNode_t dep, CgArgs* a, const S
         return n1;
     }
     if (ap.levels) {
-        add_kernel(g, &n1, &dep, 1, ic0_level_sweep<0>, kSweepCluster, a, ap.smem, kSweepThreads);
-        add_kernel(g, &n2, &n1, 1, ic0_level_sweep<1>, kSweepCluster, a, ap.smem, kSweepThreads);
+        cudaGraphNode_t n0;
+        add_kernel(g, &n0, &dep, 1, ic0_sweep_inputs<false>, a->blocks, a);
+        add_kernel(g, &n1, &n0, 1, ic0_level_sweep<0>, kSweepCluster, a, ap.smem, kSweepBlock);
+        add_kernel(g, &n2, &n1, 1, ic0_level_sweep<1>, kSweepCluster, a, ap.smem, kSweepBlock);
         return n2;
     }
     add_kernel(g, &n1, &dep, 1, ic0_forward, ap.chunks, a, 0, kSweepRows);
@@ -1690,14 +1701,16 @@ void launch_separate_unrolled(cudaStream_t stream, CgArgs* a, int blocks, const 
             return;
         }
         if (ap.levels) {
-            ic0_level_sweep<0><<<kSweepCluster, kSweepThreads, ap.smem, stream>>>(*a);
+            ic0_sweep_inputs<false><<<a->blocks, kThreads, 0, stream>>>(*a);
+            LF_CUDA(cudaGetLastError());
+            ic0_level_sweep<0><<<kSweepCluster, kSweepBlock, ap.smem, stream>>>(*a);
         } else {
             ic0_forward<<<ap.chunks, kSweepRows, 0, stream>>>(*a);  // one CTA per chunk of kSweepRows rows
         }
         LF_CUDA(cudaGetLastError());
         trail.mark(in_loop ? 2 : -1);
         if (ap.levels) {
-            ic0_level_sweep<1><<<kSweepCluster, kSweepThreads, ap.smem, stream>>>(*a);
+            ic0_level_sweep<1><<<kSweepCluster, kSweepBlock, ap.smem, stream>>>(*a);
         } else {
             ic0_backward<<<ap.chunks, kSweepRows, 0, stream>>>(*a);
         }
@@ -1739,6 +1752,7 @@ SeparateApply sweep_args(Context& c, CgArgs& a, bool fp32) {
     for (int d = 0; d < 2; ++d) {
         const Context::Sweep& s = c.sweep[d];
         a.sw[d].level_begin = s.level_begin;
+        a.sw[d].pieces = s.pieces;
         a.sw[d].desc = s.desc;
         a.sw[d].dep = s.dep;
         a.sw[d].val = fp32 ? static_cast<const void*>(s.val32.p) : static_cast<const void*>(s.val.p);
@@ -1746,18 +1760,26 @@ SeparateApply sweep_args(Context& c, CgArgs& a, bool fp32) {
         a.sw[d].levels = s.levels;
     }
     a.sw_window = c.sweep_window;
+    a.sw_maxp = c.sweep_maxp;
+    a.sw_maxe = c.sweep_maxe;
     SeparateApply ap{};
     ap.levels = true;
     if (fp32) {
-        c.sweep_y32.ensure(c.n);
+        c.sweep_y32.ensure(c.n + kSweepSlack);
+        c.sweep_rhs32.ensure(c.n + kSweepSlack);
+        c.sweep_rr32.ensure(c.n + kSweepSlack);
         a.sw_y = c.sweep_y32.p;
-        ap.smem = c.sweep_window * static_cast<int>(sizeof(float));
+        a.sw_rhs = c.sweep_rhs32.p;
+        a.sw_rr = c.sweep_rr32.p;
+        ap.smem = sweep_smem_bytes(static_cast<int>(sizeof(float)), c.sweep_window, c.sweep_maxp, c.sweep_maxe);
         LF_CUDA(cudaFuncSetAttribute(ic0_level_sweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ap.smem));
         LF_CUDA(cudaFuncSetAttribute(ic0_level_sweep<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, ap.smem));
     } else {
-        c.sweep_y.ensure(c.n);
+        c.sweep_y.ensure(c.n + kSweepSlack);
+        c.sweep_rhs.ensure(c.n + kSweepSlack);
         a.sw_y = c.sweep_y.p;
-        ap.smem = c.sweep_window * static_cast<int>(sizeof(double));
+        a.sw_rhs = c.sweep_rhs.p;
+        ap.smem = sweep_smem_bytes(static_cast<int>(sizeof(double)), c.sweep_window, c.sweep_maxp, c.sweep_maxe);
         LF_CUDA(cudaFuncSetAttribute(ic0_level_sweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, ap.smem));
         LF_CUDA(cudaFuncSetAttribute(ic0_level_sweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ap.smem));
     }
@@ -1923,15 +1945,19 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     // of every pass.
     // IC(0): residual (warm start), init, two sweeps and start, then six kernels a
     // pass; subdomain block-Jacobi: one apply kernel in place of the two sweeps.
-    if (s.precond == LFGPU_PRECOND_IC0 && s.mixed)  // mixed: init + two sweeps, then product, update and two
-                                                    // sweeps an iteration, flush and residual per replacement,
-                                                    // final flush
-        c.launches += 3 + (s.unrolled > 0 ? 6 * static_cast<i64>(s.unrolled)
-                                          : 4 * kBodyIterations * ((st.it + kBodyIterations - 1) / kBodyIterations) +
+    // IC(0) by levels: a gather of r (ic0_sweep_inputs) before the two sweeps.
+    const bool levels = c.ic0_sweep != LFGPU_IC0_SWEEP_POLLED && c.sweep_window > 0 &&
+                        c.sweep_pattern_version == c.pattern_version;
+    if (s.precond == LFGPU_PRECOND_IC0 && s.mixed)  // mixed: init, gather and two sweeps, then product, update,
+                                                    // gather and two sweeps an iteration, flush and residual per
+                                                    // replacement, final flush
+        c.launches += 4 + (s.unrolled > 0 ? 7 * static_cast<i64>(s.unrolled)
+                                          : 5 * kBodyIterations * ((st.it + kBodyIterations - 1) / kBodyIterations) +
                                                 2 * st.refs) +
                       1;
     else if (s.precond == LFGPU_PRECOND_IC0)
-        c.launches += (s.x0 ? 1 : 0) + 4 + 6 * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
+        c.launches += (s.x0 ? 1 : 0) + (levels ? 5 : 4) +
+                      (levels ? 7 : 6) * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
     else if (s.precond == LFGPU_PRECOND_SUBDOMAIN && !s.mixed)
         c.launches += (s.x0 ? 1 : 0) + 3 + 5 * (s.unrolled > 0 ? static_cast<i64>(s.unrolled) : st.it);
     else if (s.precond == LFGPU_PRECOND_SUBDOMAIN)  // mixed: init + apply, then product, update, apply an
@@ -2082,10 +2108,12 @@ void launch_precond_apply(Context& c, int precond, const double* r, double* z) {
         LF_CUDA(cudaMemsetAsync(c.cg_state.p, 0, sizeof(CgState), c.stream));
         ensure_ic0_sweep_values(c, false);
         const SeparateApply ap = sweep_args(c, a, false);
-        ic0_level_sweep<0><<<kSweepCluster, kSweepThreads, ap.smem, c.stream>>>(a);
+        ic0_sweep_inputs<false><<<blocks, kThreads, 0, c.stream>>>(a);
         LF_CUDA(cudaGetLastError());
-        ic0_level_sweep<1><<<kSweepCluster, kSweepThreads, ap.smem, c.stream>>>(a);
-        c.launches += 2;
+        ic0_level_sweep<0><<<kSweepCluster, kSweepBlock, ap.smem, c.stream>>>(a);
+        LF_CUDA(cudaGetLastError());
+        ic0_level_sweep<1><<<kSweepCluster, kSweepBlock, ap.smem, c.stream>>>(a);
+        c.launches += 3;
     } else if (precond == LFGPU_PRECOND_IC0) {
         // The sweeps read the done flag of a solver state: give them a fresh one.
         c.cg_state.ensure(sizeof(CgState));

@@ -235,6 +235,7 @@ struct Context {
     struct Sweep {
         int levels = 0, entries = 0;
         Buf<int> level_begin;  // 2 per level + 2: first position, first entry
+        Buf<int4> pieces;      // per level and cluster CTA: first and end position, first and end entry
         Buf<int4> desc;        // per position: row, first entry, end entry, output index
         Buf<int> dep;          // per entry: position of the row it depends on
         Buf<double> val, inv;  // factor entries and reciprocal pivots in schedule order
@@ -245,8 +246,9 @@ struct Context {
     unsigned long long sweep_pattern_version = ~0ull;
     int sweep_window = 0;             // ring slots (a power of two); 0: the schedule does not fit
     i64 sweep_max_width = 0, sweep_max_distance = 0;
-    Buf<double> sweep_y;              // forward result, in backward positions
-    Buf<float> sweep_y32;
+    int sweep_maxp = 0, sweep_maxe = 0;  // the largest piece a CTA takes of a level: rows, entries
+    Buf<double> sweep_y, sweep_rhs;   // forward result in backward positions; r in forward positions
+    Buf<float> sweep_y32, sweep_rhs32, sweep_rr32;  // the same in FP32; r32 in backward positions
 
     // Options (lfgpu_set_option).
     unsigned long long wait_limit_ns = kWaitLimitNs;

@@ -249,6 +249,9 @@ void ensure_ic0_schedule(Context& c) {
     long long need = 0;
     c.sweep_max_width = 0;
     c.sweep_max_distance = 0;
+    c.sweep_maxp = 0;
+    c.sweep_maxe = 0;
+    std::vector<int> pieces;
     for (int d = 0; d < 2; ++d) {
         const SweepSchedule& s = *both[d];
         // Slots a level overwrites must hold no row a CTA still reads; CTAs run at
@@ -262,7 +265,7 @@ void ensure_ic0_schedule(Context& c) {
         dst.entries = static_cast<int>(s.dep.size());
         dst.level_begin.ensure(s.level_begin.size());
         dst.desc.ensure(static_cast<size_t>(n));
-        dst.dep.ensure(std::max<size_t>(1, s.dep.size()));
+        dst.dep.ensure(s.dep.size() + kSweepSlack);
         LF_CUDA(cudaMemcpyAsync(dst.level_begin.p, s.level_begin.data(), sizeof(int) * s.level_begin.size(),
                                 cudaMemcpyHostToDevice, c.stream));
         LF_CUDA(cudaMemcpyAsync(dst.desc.p, s.desc.data(), sizeof(int) * s.desc.size(), cudaMemcpyHostToDevice,
@@ -270,11 +273,41 @@ void ensure_ic0_schedule(Context& c) {
         if (!s.dep.empty())
             LF_CUDA(cudaMemcpyAsync(dst.dep.p, s.dep.data(), sizeof(int) * s.dep.size(), cudaMemcpyHostToDevice,
                                     c.stream));
+        // Each level's rows split into kSweepCluster contiguous pieces, one per
+        // cluster CTA: first and end position, first and end entry.
+        pieces.assign(4 * static_cast<size_t>(s.levels) * kSweepCluster, 0);
+        for (int L = 0; L < s.levels; ++L) {
+            const int p0 = s.level_begin[2 * static_cast<size_t>(L)], p1 = s.level_begin[2 * static_cast<size_t>(L) + 2];
+            const int chunk = (p1 - p0 + kSweepCluster - 1) / kSweepCluster;
+            for (int k = 0; k < kSweepCluster; ++k) {
+                const int first = std::min(p1, p0 + k * chunk), end = std::min(p1, first + chunk);
+                int* pc = &pieces[4 * (static_cast<size_t>(L) * kSweepCluster + k)];
+                pc[0] = first;
+                pc[1] = end;
+                pc[2] = first < end ? s.desc[4 * static_cast<size_t>(first) + 1] : 0;
+                pc[3] = first < end ? s.desc[4 * static_cast<size_t>(end - 1) + 2] : 0;
+                c.sweep_maxp = std::max(c.sweep_maxp, end - first);
+                c.sweep_maxe = std::max(c.sweep_maxe, pc[3] - pc[2]);
+            }
+        }
+        dst.pieces.ensure(std::max<size_t>(1, pieces.size() / 4));
+        if (!pieces.empty())
+            LF_CUDA(cudaMemcpyAsync(dst.pieces.p, pieces.data(), sizeof(int) * pieces.size(), cudaMemcpyHostToDevice,
+                                    c.stream));
+        LF_CUDA(cudaStreamSynchronize(c.stream));  // `pieces` is refilled for the other sweep
         dst.val_version = dst.val32_version = ~0ull;
     }
     int window = 256;
     while (window < need && window <= kSweepRingMax) window *= 2;
     c.sweep_window = window <= kSweepRingMax ? window : 0;
+    // Both precisions' rings and stages must fit one CTA's shared memory.
+    int optin = 0;
+    LF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
+    if (c.sweep_window > 0 &&
+        sweep_smem_bytes(static_cast<int>(sizeof(double)), c.sweep_window, c.sweep_maxp, c.sweep_maxe) +
+                kSweepStaticSmem >
+            optin)
+        c.sweep_window = 0;
     LF_CUDA(cudaStreamSynchronize(c.stream));  // the host schedules are released on return
     c.sweep_pattern_version = c.pattern_version;
 }
@@ -286,16 +319,16 @@ void ensure_ic0_sweep_values(Context& c, bool fp32) {
         Context::Sweep& s = c.sweep[d];
         const int total = s.entries;
         if (s.val_version != c.ic0_version) {
-            s.val.ensure(std::max(1, total));
-            s.inv.ensure(n);
+            s.val.ensure(static_cast<size_t>(total) + kSweepSlack);
+            s.inv.ensure(static_cast<size_t>(n) + kSweepSlack);
             ic0_schedule_values_kernel<double><<<grid, kThreads, 0, c.stream>>>(
                 n, d == 0, s.desc, c.rowptr, c.diag, c.ic0_val, c.ic0_inv, s.val, s.inv);
             c.launches += 1;
             s.val_version = c.ic0_version;
         }
         if (fp32 && s.val32_version != c.ic0_version) {
-            s.val32.ensure(std::max(1, total));
-            s.inv32.ensure(n);
+            s.val32.ensure(static_cast<size_t>(total) + kSweepSlack);
+            s.inv32.ensure(static_cast<size_t>(n) + kSweepSlack);
             ic0_schedule_values_kernel<float><<<grid, kThreads, 0, c.stream>>>(
                 n, d == 0, s.desc, c.rowptr, c.diag, c.ic0_val, c.ic0_inv, s.val32, s.inv32);
             c.launches += 1;

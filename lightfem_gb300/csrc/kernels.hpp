@@ -79,12 +79,49 @@ void ensure_ic0_sweep_values(Context& c, bool fp32);
 bool ic0_use_levels(Context& c, bool required);
 
 // The level-scheduled sweeps run as one cluster of kSweepCluster CTAs of
-// kSweepThreads threads; every CTA keeps a ring of the last sweep_window results
-// in shared memory (kSweepStages mbarriers track the levels in flight).
+// kSweepThreads consumer threads and a producer warp; every CTA keeps a ring of
+// the last sweep_window results in shared memory and kSweepStages stages of
+// operands, each one CTA's piece of one level (copied in by TMA).
 constexpr int kSweepCluster = 8;
 constexpr int kSweepThreads = 128;
-constexpr int kSweepStages = 4;
+constexpr int kSweepStages = 8;
 constexpr int kSweepRingMax = 16384;
+
+#ifdef __CUDACC__
+#define LF_HD __host__ __device__
+#else
+#define LF_HD
+#endif
+
+LF_HD inline int sweep_round16(int bytes) { return (bytes + 15) & ~15; }
+
+// Byte offsets of a stage's arrays and its size, for elements of `elem` bytes and
+// pieces of at most maxp rows and maxe entries.  Arrays that do not start on a
+// 16-byte boundary are copied from the boundary below their start (TMA copies
+// whole 16-byte units), hence the slack.
+struct SweepStageLayout {
+    int desc, dep, val, inv, rhs, rr, bytes;
+};
+LF_HD inline SweepStageLayout sweep_stage_layout(int elem, int maxp, int maxe) {
+    SweepStageLayout l;
+    l.desc = 0;
+    l.dep = l.desc + sweep_round16(maxp * 16);
+    l.val = l.dep + sweep_round16((maxe + 8) * 4);
+    l.inv = l.val + sweep_round16((maxe + 8) * elem);
+    l.rhs = l.inv + sweep_round16((maxp + 8) * elem);
+    l.rr = l.rhs + sweep_round16((maxp + 8) * elem);
+    l.bytes = l.rr + sweep_round16((maxp + 8) * elem);
+    return l;
+}
+// Dynamic shared memory of a level sweep: the ring of `window` results, then the stages.
+LF_HD inline int sweep_smem_bytes(int elem, int window, int maxp, int maxe) {
+    return sweep_round16(window * elem) + kSweepStages * sweep_stage_layout(elem, maxp, maxe).bytes;
+}
+// Shared memory a sweep CTA may use beyond its dynamic part (barriers, pieces, reductions).
+constexpr int kSweepStaticSmem = 4096;
+// Elements allocated past the end of every array a sweep copies by TMA: a copy
+// rounded up to whole 16-byte units reads up to three elements beyond its range.
+constexpr int kSweepSlack = 16;
 
 // pattern.cu: CSR pattern and element->value map on the device; false if a node
 // has more elements than the device build handles (the caller builds on the host)
