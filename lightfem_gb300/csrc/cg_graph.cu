@@ -97,7 +97,8 @@ struct CgArgs {
     // IC(0) level-scheduled sweeps (ic0.cu builds the schedules): [0] forward, [1] backward
     struct SweepPlan {
         const int* level_begin;    // 2 per level + 2: first position, first entry
-        const int4* pieces;        // per level and CTA: first and end position, first and end entry
+        const int4* pieces;        // per level and CTA, two int4: first and end position, first and end
+                                   // entry; the width of level L - 1 + kSweepRingBars (-1: none)
         const int4* desc;          // per position: row, first entry, end entry, output index
         const int* dep;            // per entry: position of the row it depends on
         const void* val;           // factor entries in schedule order (double or float)
@@ -987,7 +988,7 @@ __global__ void __launch_bounds__(kSweepRows) ic0_backward(CgArgs a) {
 // forward sweep reads r in schedule order (ic0_sweep_inputs gathers it first), the
 // backward sweep the forward result, which the forward sweep writes in backward
 // order.
-constexpr int kSweepRingBars = 4;
+constexpr int kSweepUnroll = 12;                // entries of a row whose products are formed together
 constexpr int kSweepConsumers = kSweepThreads;   // one row per consumer thread and pass
 constexpr int kSweepBlock = kSweepThreads + 32;  // plus the producer warp
 
@@ -1041,10 +1042,13 @@ __device__ __forceinline__ void consumers_sync() {
     asm volatile("bar.sync 1, %0;" ::"n"(kSweepConsumers) : "memory");
 }
 
-__device__ __forceinline__ double sweep_term(double acc, double l, double v) { return __dsub_rn(acc, __dmul_rn(l, v)); }
-__device__ __forceinline__ float sweep_term(float acc, float l, float v) { return __fsub_rn(acc, __fmul_rn(l, v)); }
-__device__ __forceinline__ double sweep_scale(double acc, double inv) { return __dmul_rn(acc, inv); }
-__device__ __forceinline__ float sweep_scale(float acc, float inv) { return __fmul_rn(acc, inv); }
+// A row's terms: each product rounded on its own, then subtracted in order.  The
+// products do not depend on one another, so they are formed together and only the
+// subtractions form the row's dependency chain.
+__device__ __forceinline__ double sweep_mul(double l, double v) { return __dmul_rn(l, v); }
+__device__ __forceinline__ float sweep_mul(float l, float v) { return __fmul_rn(l, v); }
+__device__ __forceinline__ double sweep_sub(double acc, double t) { return __dsub_rn(acc, t); }
+__device__ __forceinline__ float sweep_sub(float acc, float t) { return __fsub_rn(acc, t); }
 
 // rho and beta from r.z after a separate preconditioner application (the mixed
 // loop's subdomain and IC(0) forms): the first rho after mx_init, then beta =
@@ -1097,6 +1101,7 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
     extern __shared__ __align__(128) unsigned char sweep_smem[];
     __shared__ __align__(8) unsigned long long full[S], empty[S], ringbar[SR];
     __shared__ int4 piece_of[S];
+    __shared__ int rearm_of[S];
     __shared__ int s_failed;
     const CgArgs::SweepPlan& sp = a.sw[kFwd ? 0 : 1];
     const int levels = sp.levels;
@@ -1124,40 +1129,73 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
     bool ok = true;
     FloatPair rz;  // the mixed backward sweep's r.z (zero on the producer warp)
     if (tid >= kSweepConsumers) {
-        // ---- producer warp: one lane copies each level's piece into its stage.
-        if (tid == kSweepConsumers) {
-            const unsigned long long policy = l2_evict_first_policy();
-            const T* rhs_src = static_cast<const T*>(kFwd ? a.sw_rhs : a.sw_y);
-            for (int L = 0; L < levels; ++L) {
+        // ---- producer warp: one lane copies each level's piece into its stage.  The
+        // warp reads the piece table 32 levels at a time (lane i: level base + i),
+        // one batch ahead, so no copy waits on a table load.
+        const int lane = tid & 31;
+        const unsigned long long policy = l2_evict_first_policy();
+        const T* rhs_src = static_cast<const T*>(kFwd ? a.sw_rhs : a.sw_y);
+        const int4 none = make_int4(0, 0, 0, 0);
+        auto batch = [&](int base, int4& pc, int& rearm) {
+            const int L = base + lane;
+            pc = none;
+            rearm = -1;
+            if (L < levels) {
+                const int4* e = sp.pieces + 2 * (static_cast<size_t>(L) * kSweepCluster + rank);
+                pc = __ldg(e);
+                rearm = __ldg(e + 1).x;
+            }
+        };
+        int4 cur_pc, next_pc;
+        int cur_rearm, next_rearm;
+        batch(0, cur_pc, cur_rearm);
+        batch(32, next_pc, next_rearm);
+        for (int L = 0; L < levels; ++L) {
+            const int i = L & 31;
+            if (i == 0 && L > 0) {
+                cur_pc = next_pc;
+                cur_rearm = next_rearm;
+                batch(L + 32, next_pc, next_rearm);
+            }
+            int4 pc;
+            pc.x = __shfl_sync(0xffffffffu, cur_pc.x, i);
+            pc.y = __shfl_sync(0xffffffffu, cur_pc.y, i);
+            pc.z = __shfl_sync(0xffffffffu, cur_pc.z, i);
+            pc.w = __shfl_sync(0xffffffffu, cur_pc.w, i);
+            const int rearm = __shfl_sync(0xffffffffu, cur_rearm, i);
+            if (lane == 0) {
                 const int s = L % S;
                 // The stage is free once the consumers are done with level L - S.
                 if (L >= S) ok = wait_phase(empty + s, static_cast<unsigned>(L / S - 1) & 1u, a.status, L) && ok;
-                const int4 pc = __ldg(sp.pieces + static_cast<size_t>(L) * kSweepCluster + rank);
                 piece_of[s] = pc;
+                rearm_of[s] = rearm;
                 unsigned char* st = stages + static_cast<size_t>(s) * lay.bytes;
                 const int cnt = pc.y - pc.x;
                 if (cnt <= 0) {
                     mbar_expect_tx(full + s, 0u);  // an empty piece: the phase completes at once
-                    continue;
+                } else {
+                    const int dep0 = pc.z - lead_of<int>(pc.z), val0 = pc.z - lead_of<T>(pc.z);
+                    const int pos0 = pc.x - lead_of<T>(pc.x);
+                    const bool entries = pc.w > pc.z;
+                    const unsigned b_desc = static_cast<unsigned>(cnt) * 16u;
+                    const unsigned b_dep = entries ? static_cast<unsigned>(sweep_round16((pc.w - dep0) * 4)) : 0u;
+                    const unsigned b_val =
+                        entries ? static_cast<unsigned>(sweep_round16((pc.w - val0) * static_cast<int>(sizeof(T))))
+                                : 0u;
+                    const unsigned b_pos =
+                        static_cast<unsigned>(sweep_round16((pc.y - pos0) * static_cast<int>(sizeof(T))));
+                    mbar_expect_tx(full + s, b_desc + b_dep + b_val + (MODE == 3 ? 3u : 2u) * b_pos);
+                    bulk_copy(st + lay.desc, sp.desc + pc.x, b_desc, full + s, policy);
+                    if (entries) {
+                        bulk_copy(st + lay.dep, sp.dep + dep0, b_dep, full + s, policy);
+                        bulk_copy(st + lay.val, static_cast<const T*>(sp.val) + val0, b_val, full + s, policy);
+                    }
+                    bulk_copy(st + lay.inv, static_cast<const T*>(sp.inv) + pos0, b_pos, full + s, policy);
+                    bulk_copy(st + lay.rhs, rhs_src + pos0, b_pos, full + s, policy);
+                    if (MODE == 3) bulk_copy(st + lay.rr, a.sw_rr + pos0, b_pos, full + s, policy);
                 }
-                const int dep0 = pc.z - lead_of<int>(pc.z), val0 = pc.z - lead_of<T>(pc.z);
-                const int pos0 = pc.x - lead_of<T>(pc.x);
-                const bool entries = pc.w > pc.z;
-                const unsigned b_desc = static_cast<unsigned>(cnt) * 16u;
-                const unsigned b_dep = entries ? static_cast<unsigned>(sweep_round16((pc.w - dep0) * 4)) : 0u;
-                const unsigned b_val =
-                    entries ? static_cast<unsigned>(sweep_round16((pc.w - val0) * static_cast<int>(sizeof(T)))) : 0u;
-                const unsigned b_pos = static_cast<unsigned>(sweep_round16((pc.y - pos0) * static_cast<int>(sizeof(T))));
-                mbar_expect_tx(full + s, b_desc + b_dep + b_val + (MODE == 3 ? 3u : 2u) * b_pos);
-                bulk_copy(st + lay.desc, sp.desc + pc.x, b_desc, full + s, policy);
-                if (entries) {
-                    bulk_copy(st + lay.dep, sp.dep + dep0, b_dep, full + s, policy);
-                    bulk_copy(st + lay.val, static_cast<const T*>(sp.val) + val0, b_val, full + s, policy);
-                }
-                bulk_copy(st + lay.inv, static_cast<const T*>(sp.inv) + pos0, b_pos, full + s, policy);
-                bulk_copy(st + lay.rhs, rhs_src + pos0, b_pos, full + s, policy);
-                if (MODE == 3) bulk_copy(st + lay.rr, a.sw_rr + pos0, b_pos, full + s, policy);
             }
+            __syncwarp();
         }
     } else {
         // ---- consumers: one row per thread and pass.
@@ -1169,10 +1207,6 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
         }
         for (int L = 0; L < levels; ++L) {
             const int s = L % S;
-            // Bytes the ring mbarrier of level L - 1 expects when it is armed again,
-            // for level L - 1 + SR, at the end of this level: loaded now, used then.
-            const bool rearm = tid == 0 && L > 0 && L - 1 + SR < levels;
-            const unsigned rearm_bytes = rearm ? width_bytes(L - 1 + SR) : 0u;
             ok = wait_phase(full + s, static_cast<unsigned>(L / S) & 1u, a.status, L) && ok;
             if (L > 0) {
                 const int prev = L - 1;
@@ -1193,8 +1227,20 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
                 const int p = pc.x + t;
                 const int4 d = sdesc[t];
                 T acc = srhs[p - pos0];
-                for (int j = d.y; j < d.z; ++j) acc = sweep_term(acc, sval[j - val0], ring[sdep[j - dep0] & mask]);
-                const T y = sweep_scale(acc, sinv[p - pos0]);
+                const int nj = d.z - d.y;
+                if (nj <= kSweepUnroll) {
+                    T prod[kSweepUnroll];
+#pragma unroll
+                    for (int k = 0; k < kSweepUnroll; ++k)
+                        if (k < nj) prod[k] = sweep_mul(sval[d.y + k - val0], ring[sdep[d.y + k - dep0] & mask]);
+#pragma unroll
+                    for (int k = 0; k < kSweepUnroll; ++k)
+                        if (k < nj) acc = sweep_sub(acc, prod[k]);
+                } else {
+                    for (int j = d.y; j < d.z; ++j)
+                        acc = sweep_sub(acc, sweep_mul(sval[j - val0], ring[sdep[j - dep0] & mask]));
+                }
+                const T y = sweep_mul(acc, sinv[p - pos0]);
                 const unsigned slot = static_cast<unsigned>(p & mask) * static_cast<unsigned>(sizeof(T));
 #pragma unroll
                 for (int k = 0; k < kSweepCluster; ++k) store_remote(ring_at[k] + slot, y, bar_at[k] + bar_off);
@@ -1210,8 +1256,11 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
             }
             consumers_sync();  // every consumer is done with stage s and has seen level L - 1 arrive
             if (tid == 0) {
+                // The ring mbarrier of level L - 1 is free again: armed for level
+                // L - 1 + SR, whose width the piece table carries with level L.
+                const int rearm = rearm_of[s];
                 arrive(empty + s);
-                if (rearm) mbar_expect_tx(ringbar + (L - 1) % SR, rearm_bytes);
+                if (rearm >= 0) mbar_expect_tx(ringbar + (L - 1) % SR, static_cast<unsigned>(rearm) * sizeof(T));
             }
         }
         // Every result bound for this CTA has arrived before it exits.

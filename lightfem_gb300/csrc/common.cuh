@@ -235,7 +235,8 @@ struct Context {
     struct Sweep {
         int levels = 0, entries = 0;
         Buf<int> level_begin;  // 2 per level + 2: first position, first entry
-        Buf<int4> pieces;      // per level and cluster CTA: first and end position, first and end entry
+        Buf<int4> pieces;      // per level and cluster CTA, two int4: first and end position, first and
+                               // and end entry, then the width of a level ahead (see ic0.cu)
         Buf<int4> desc;        // per position: row, first entry, end entry, output index
         Buf<int> dep;          // per entry: position of the row it depends on
         Buf<double> val, inv;  // factor entries and reciprocal pivots in schedule order

@@ -274,23 +274,29 @@ void ensure_ic0_schedule(Context& c) {
             LF_CUDA(cudaMemcpyAsync(dst.dep.p, s.dep.data(), sizeof(int) * s.dep.size(), cudaMemcpyHostToDevice,
                                     c.stream));
         // Each level's rows split into kSweepCluster contiguous pieces, one per
-        // cluster CTA: first and end position, first and end entry.
-        pieces.assign(4 * static_cast<size_t>(s.levels) * kSweepCluster, 0);
+        // cluster CTA: first and end position, first and end entry; then the width
+        // of level L - 1 + kSweepRingBars, whose ring mbarrier is armed at the end
+        // of level L (-1: none).
+        pieces.assign(8 * static_cast<size_t>(s.levels) * kSweepCluster, 0);
         for (int L = 0; L < s.levels; ++L) {
             const int p0 = s.level_begin[2 * static_cast<size_t>(L)], p1 = s.level_begin[2 * static_cast<size_t>(L) + 2];
             const int chunk = (p1 - p0 + kSweepCluster - 1) / kSweepCluster;
             for (int k = 0; k < kSweepCluster; ++k) {
                 const int first = std::min(p1, p0 + k * chunk), end = std::min(p1, first + chunk);
-                int* pc = &pieces[4 * (static_cast<size_t>(L) * kSweepCluster + k)];
+                int* pc = &pieces[8 * (static_cast<size_t>(L) * kSweepCluster + k)];
                 pc[0] = first;
                 pc[1] = end;
                 pc[2] = first < end ? s.desc[4 * static_cast<size_t>(first) + 1] : 0;
                 pc[3] = first < end ? s.desc[4 * static_cast<size_t>(end - 1) + 2] : 0;
+                const int ahead = L - 1 + kSweepRingBars;
+                pc[4] = L > 0 && ahead < s.levels
+                            ? s.level_begin[2 * static_cast<size_t>(ahead) + 2] - s.level_begin[2 * static_cast<size_t>(ahead)]
+                            : -1;
                 c.sweep_maxp = std::max(c.sweep_maxp, end - first);
                 c.sweep_maxe = std::max(c.sweep_maxe, pc[3] - pc[2]);
             }
         }
-        dst.pieces.ensure(std::max<size_t>(1, pieces.size() / 4));
+        dst.pieces.ensure(std::max<size_t>(2, pieces.size() / 4));
         if (!pieces.empty())
             LF_CUDA(cudaMemcpyAsync(dst.pieces.p, pieces.data(), sizeof(int) * pieces.size(), cudaMemcpyHostToDevice,
                                     c.stream));

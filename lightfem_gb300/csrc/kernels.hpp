@@ -85,6 +85,7 @@ bool ic0_use_levels(Context& c, bool required);
 constexpr int kSweepCluster = 8;
 constexpr int kSweepThreads = 128;
 constexpr int kSweepStages = 8;
+constexpr int kSweepRingBars = 4;  // mbarriers cycling over the levels whose results are in flight
 constexpr int kSweepRingMax = 16384;
 
 #ifdef __CUDACC__
