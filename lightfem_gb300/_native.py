@@ -12,7 +12,9 @@ from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_void_
 
 import numpy as np
 
-LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "liblfgpu.so")
+# The in-tree build; LFGPU_LIBRARY names another build of the same sources.
+LIB_PATH = os.environ.get("LFGPU_LIBRARY") or os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib",
+                                                           "liblfgpu.so")
 
 # enums of include/lfgpu.h
 OK = 0

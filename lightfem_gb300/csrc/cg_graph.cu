@@ -1205,13 +1205,11 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
             ring_at[k] = cluster_address(smem_u32(ring), k);
             bar_at[k] = cluster_address(smem_u32(ringbar), k);
         }
+        // The (z, p) copy the next product reads (the mixed backward sweep's output).
+        float* zp_out = MODE == 3 ? reinterpret_cast<float*>(zp_buffer(a, a.st->it)) : nullptr;
         for (int L = 0; L < levels; ++L) {
             const int s = L % S;
             ok = wait_phase(full + s, static_cast<unsigned>(L / S) & 1u, a.status, L) && ok;
-            if (L > 0) {
-                const int prev = L - 1;
-                ok = wait_phase(ringbar + prev % SR, static_cast<unsigned>(prev / SR) & 1u, a.status, prev) && ok;
-            }
             const int4 pc = piece_of[s];
             const unsigned char* st = stages + static_cast<size_t>(s) * lay.bytes;
             const int4* sdesc = reinterpret_cast<const int4*>(st + lay.desc);
@@ -1223,24 +1221,9 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
             const T* srhs = reinterpret_cast<const T*>(st + lay.rhs);
             const T* srr = reinterpret_cast<const T*>(st + lay.rr);
             const unsigned bar_off = static_cast<unsigned>(L % SR) * 8u;
-            for (int t = tid; t < pc.y - pc.x; t += kSweepConsumers) {
-                const int p = pc.x + t;
-                const int4 d = sdesc[t];
-                T acc = srhs[p - pos0];
-                const int nj = d.z - d.y;
-                if (nj <= kSweepUnroll) {
-                    T prod[kSweepUnroll];
-#pragma unroll
-                    for (int k = 0; k < kSweepUnroll; ++k)
-                        if (k < nj) prod[k] = sweep_mul(sval[d.y + k - val0], ring[sdep[d.y + k - dep0] & mask]);
-#pragma unroll
-                    for (int k = 0; k < kSweepUnroll; ++k)
-                        if (k < nj) acc = sweep_sub(acc, prod[k]);
-                } else {
-                    for (int j = d.y; j < d.z; ++j)
-                        acc = sweep_sub(acc, sweep_mul(sval[j - val0], ring[sdep[j - dep0] & mask]));
-                }
-                const T y = sweep_mul(acc, sinv[p - pos0]);
+            const int cnt = pc.y - pc.x;
+            // The result of a row: into every CTA's ring, and out.
+            auto publish = [&](int p, const int4& d, T y, T r) {
                 const unsigned slot = static_cast<unsigned>(p & mask) * static_cast<unsigned>(sizeof(T));
 #pragma unroll
                 for (int k = 0; k < kSweepCluster; ++k) store_remote(ring_at[k] + slot, y, bar_at[k] + bar_off);
@@ -1250,9 +1233,55 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
                     a.z[d.x] = y;
                 } else {
                     // z of DOF 2m sits in .x of node m's (z, p) float4, z of DOF 2m + 1 in .z.
-                    reinterpret_cast<float*>(zp_buffer(a, a.st->it))[4 * (d.x >> 1) + 2 * (d.x & 1)] = y;
-                    rz.add(srr[p - pos0] * y);
+                    zp_out[4 * (d.x >> 1) + 2 * (d.x & 1)] = y;
+                    rz.add(r * y);
                 }
+            };
+            // This thread's first row: its operands come out of the stage before the
+            // wait for level L - 1, so only the ring reads and the arithmetic follow it.
+            const bool have = tid < cnt;
+            int4 d = make_int4(0, 0, 0, 0);
+            T rhs = T(0), inv = T(0), rr = T(0);
+            int dk[kSweepUnroll];
+            T vk[kSweepUnroll];
+            if (have) {
+                d = sdesc[tid];
+                rhs = srhs[pc.x + tid - pos0];
+                inv = sinv[pc.x + tid - pos0];
+                if constexpr (MODE == 3) rr = srr[pc.x + tid - pos0];
+#pragma unroll
+                for (int k = 0; k < kSweepUnroll; ++k) {
+                    if (d.y + k < d.z) {
+                        dk[k] = sdep[d.y + k - dep0] & mask;
+                        vk[k] = sval[d.y + k - val0];
+                    }
+                }
+            }
+            if (L > 0) {
+                const int prev = L - 1;
+                ok = wait_phase(ringbar + prev % SR, static_cast<unsigned>(prev / SR) & 1u, a.status, prev) && ok;
+            }
+            if (have) {
+                T acc = rhs;
+                T prod[kSweepUnroll];
+#pragma unroll
+                for (int k = 0; k < kSweepUnroll; ++k)
+                    if (d.y + k < d.z) prod[k] = sweep_mul(vk[k], ring[dk[k]]);
+#pragma unroll
+                for (int k = 0; k < kSweepUnroll; ++k)
+                    if (d.y + k < d.z) acc = sweep_sub(acc, prod[k]);
+                for (int j = d.y + kSweepUnroll; j < d.z; ++j)  // rows longer than the unrolled part
+                    acc = sweep_sub(acc, sweep_mul(sval[j - val0], ring[sdep[j - dep0] & mask]));
+                publish(pc.x + tid, d, sweep_mul(acc, inv), rr);
+            }
+            // Pieces wider than the consumer threads: further rows, read after the wait.
+            for (int t = tid + kSweepConsumers; t < cnt; t += kSweepConsumers) {
+                const int p = pc.x + t;
+                const int4 e = sdesc[t];
+                T acc = srhs[p - pos0];
+                for (int j = e.y; j < e.z; ++j)
+                    acc = sweep_sub(acc, sweep_mul(sval[j - val0], ring[sdep[j - dep0] & mask]));
+                publish(p, e, sweep_mul(acc, sinv[p - pos0]), MODE == 3 ? srr[p - pos0] : T(0));
             }
             consumers_sync();  // every consumer is done with stage s and has seen level L - 1 arrive
             if (tid == 0) {
