@@ -519,9 +519,12 @@ Model parse_fem_text(const std::string& text, const std::string& source_name, un
                 std::size_t e = text.find('\n', i);
                 if (e == std::string::npos || e > cut[k + 1]) e = cut[k + 1];
                 ++local;
-                std::size_t stop = e;
-                const std::size_t hash = text.find('#', i);
-                if (hash != std::string::npos && hash < stop) stop = hash;
+                // The comment starts at the line's first '#' (searched within the line only).
+                const std::size_t stop0 =
+                    static_cast<std::size_t>(std::find(text.begin() + static_cast<std::ptrdiff_t>(i),
+                                                       text.begin() + static_cast<std::ptrdiff_t>(e), '#') -
+                                             text.begin());
+                std::size_t stop = stop0;
                 std::size_t b = i;
                 while (b < stop && space(text[b])) ++b;
                 while (stop > b && space(text[stop - 1])) --stop;

@@ -3,11 +3,15 @@
 // the reference tree:
 //
 //   io_check <out_dir> <threads> <file.fem>...
+//   io_check --time <out_dir> <threads> <file.fem>
 //
 // For each file: both parsers must give the same records (every field, in order)
 // or fail with the same message; a file that parses and validates is solved with
 // the reference's solver, and both writers must write the same VTK and CSV bytes.
 // Prints one line per file ("ok ...") and exits non-zero on the first difference.
+// --time skips the solve (a large model): it fills the result with seeded values
+// of the right sizes, writes both ways, compares the bytes and prints the wall
+// time of each parse and write.
 #include "lightfem/input_parser.hpp"
 #include "lightfem/model.hpp"
 #include "lightfem/solver.hpp"
@@ -15,8 +19,10 @@
 #include "lightfem/vtk_writer.hpp"
 #include "lightfem_gpu_io.hpp"
 
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <random>
 #include <fstream>
 #include <iostream>
 #include <iterator>
@@ -96,7 +102,68 @@ std::string slurp(const std::string& path) {
 
 }  // namespace
 
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+int time_io(const std::string& out, unsigned threads, const std::string& path) {
+    auto t0 = std::chrono::steady_clock::now();
+    lightfem::Model ref = lightfem::InputParser{}.parse_file(path);
+    const double ref_parse = ms_since(t0);
+    t0 = std::chrono::steady_clock::now();
+    lightfem::Model ours = lightfem_gpu::parse_fem<lightfem::Model>(path, threads);
+    const double our_parse = ms_since(t0);
+    compare(ref, ours, path);
+    ref.sort_and_index();
+    lightfem::AnalysisResult r;
+    const std::size_t n = ref.summary().dofs;
+    std::mt19937_64 rng(7);
+    std::normal_distribution<double> g(0.0, 1e-4);
+    r.displacement.resize(n);
+    r.reaction.resize(n);
+    for (auto& v : r.displacement) v = g(rng);
+    for (auto& v : r.reaction) v = g(rng) * 1e6;
+    r.node_results.resize(ref.nodes.size());
+    for (std::size_t i = 0; i < ref.nodes.size(); ++i) {
+        r.node_results[i].node_id = ref.nodes[i].id;
+        for (auto& v : r.node_results[i].stress) v = g(rng) * 1e10;
+        r.node_results[i].von_mises = std::abs(g(rng)) * 1e10;
+    }
+    r.element_results.resize(ref.elements.size());
+    for (std::size_t e = 0; e < ref.elements.size(); ++e) {
+        auto& x = r.element_results[e];
+        x.element_id = ref.elements[e].id;
+        for (auto& v : x.field.strain) v = g(rng);
+        for (auto& v : x.field.stress) v = g(rng) * 1e10;
+        x.field.von_mises = std::abs(g(rng)) * 1e10;
+        for (auto& p : x.gauss_points) {
+            p.xi = g(rng);
+            p.eta = g(rng);
+            for (auto& v : p.field.strain) v = g(rng);
+            for (auto& v : p.field.stress) v = g(rng) * 1e10;
+            p.field.von_mises = std::abs(g(rng)) * 1e10;
+        }
+    }
+    t0 = std::chrono::steady_clock::now();
+    lightfem::write_vtk(ref, r, out + "/time_ref.vtk");
+    const auto rp = lightfem::write_csv_results(ref, r, out + "/time_ref");
+    const double ref_write = ms_since(t0);
+    t0 = std::chrono::steady_clock::now();
+    lightfem_gpu::write_vtk(ref, r, out + "/time_gpu.vtk", threads);
+    const auto gp = lightfem_gpu::write_csv_results(ref, r, out + "/time_gpu", threads);
+    const double our_write = ms_since(t0);
+    if (slurp(out + "/time_ref.vtk") != slurp(out + "/time_gpu.vtk")) differ(path + ": VTK bytes");
+    if (slurp(rp.nodes) != slurp(gp.first)) differ(path + ": nodes CSV bytes");
+    if (slurp(rp.gauss_points) != slurp(gp.second)) differ(path + ": Gauss-point CSV bytes");
+    std::printf("{\"nodes\": %zu, \"threads\": %u, \"parse_ms\": {\"reference\": %.1f, \"threaded\": %.1f}, "
+                "\"write_ms\": {\"reference\": %.1f, \"threaded\": %.1f}, \"identical\": %s}\n",
+                ref.nodes.size(), threads, ref_parse, our_parse, ref_write, our_write, failures ? "false" : "true");
+    return failures == 0 ? 0 : 1;
+}
+
 int main(int argc, char** argv) {
+    if (argc == 5 && std::string(argv[1]) == "--time")
+        return time_io(argv[2], static_cast<unsigned>(std::atoi(argv[3])), argv[4]);
     if (argc < 4) {
         std::cerr << "usage: io_check <out_dir> <threads> <file.fem>...\n";
         return 2;
