@@ -608,8 +608,7 @@ def run_ours(args) -> int:
     for prec, st, pc, pers in () if args.no_variants else (("mixed", "bsr", "block", False), ("mixed", "csr", "jacobi", False),
                                ("fp64", "csr", "jacobi", False), ("fp64", "bsr", "block", False),
                                ("mixed", "bsr", "subdomain", False),
-                               ("mixed", "csr", "ic0", False), ("mixed", "bsr", "ic0", False),
-                               ("fp64", "csr", "ic0", False),
+                               ("mixed", "csr", "ic0", False), ("fp64", "csr", "ic0", False),
                                ("mixed", "bsr", "jacobi", True), ("fp64", "csr", "jacobi", True)):
         try:
             ms, r = step(opts(prec, st, pc, pers))
