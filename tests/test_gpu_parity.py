@@ -263,7 +263,9 @@ def test_cfg2_full_size(native, golden_json, variant):
     mixed.settings.precision = "mixed"
     rm = LinearElasticSolver(retain_matrix=False, postprocess=False).solve(mixed)
     assert rm.solver.true_residual <= 1.001e-8 * rm.solver.initial_residual
-    assert rel(by_id_order(mixed, rm.displacement), u) <= 1e-6
+    # The benchmark spec's bar for u: 1e-8 relative to the FP64 solution (measured on
+    # the bench's Jacobi run: 8.4e-10).
+    assert rel(by_id_order(mixed, rm.displacement), u) <= 1e-8
 
 
 def test_cfg3_full_size_mixed_vs_fp64(native):
@@ -283,7 +285,7 @@ def test_cfg3_full_size_mixed_vs_fp64(native):
         assert np.allclose(res.reaction.reshape(-1, 2).sum(axis=0), -res.load.reshape(-1, 2).sum(axis=0),
                            rtol=1e-6, atol=1e-6 * np.abs(res.load).sum())
         sols[precision] = res.displacement
-    assert rel(sols["mixed"], sols["fp64"]) <= 1e-6
+    assert rel(sols["mixed"], sols["fp64"]) <= 1e-8
 
 
 @pytest.mark.parametrize("storage", ["csr", "bsr"])
@@ -299,9 +301,9 @@ def test_mixed_precision_reaches_fp64_target(native, storage, precond, refinemen
     assert res.solver.true_residual <= 1.001 * tol
     assert res.solver.final_residual <= tol
     assert res.solver.refinements >= 1
-    # Two solutions at a 1e-8 relative residual differ by at most cond(K) * 1e-8;
-    # the FP64 solution is the oracle here.
-    assert rel(res.displacement, fp64.displacement) <= 1e-4
+    # Two solutions at a 1e-8 relative residual may differ by up to cond(K) * 1e-8;
+    # the FP64 solution is the oracle here, and the benchmark spec's 1e-8 holds.
+    assert rel(res.displacement, fp64.displacement) <= 1e-8
 
 
 @pytest.mark.parametrize("name", ["grid6", "beam", "strain"])
@@ -481,7 +483,7 @@ def test_mixed_ic0_200x200(native, storage):
     res = LinearElasticSolver(retain_matrix=False, postprocess=False).solve(model)
     assert res.solver.converged and res.solver.fallback_fp64 == 0
     assert res.solver.true_residual <= 1.001e-8 * res.solver.initial_residual
-    assert rel(res.displacement, fp64.displacement) <= 1e-6
+    assert rel(res.displacement, fp64.displacement) <= 1e-8
 
 
 @pytest.mark.parametrize("name", ["grid6", "beam", "strain"])
