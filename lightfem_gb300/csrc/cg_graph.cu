@@ -47,6 +47,10 @@ struct CgState {
     // thread of the loop kernels converts them (GB300's FP64 pipe is narrow):
     // alpha = alpha32 + alpha32_lo to about 48 bits.
     float alpha32, alpha32_lo, beta32, pad32;
+    // Raised by the last CTA of mx_update once beta is set; the other CTAs wait for
+    // it before they form the next direction (only equality with the value a CTA
+    // saw at its start matters, so it may wrap).
+    unsigned int go, pad_go;
 };
 
 struct CgArgs {
@@ -128,9 +132,9 @@ __device__ __forceinline__ void set_branch(const CgArgs& a, bool go) {
 }
 
 // Block sums of K values, then the last block to finish adds every block's sums in
-// block order and runs fin(totals) on thread 0.
+// block order and runs fin(totals) on thread 0.  Returns true in the last block.
 template <int K, typename Final>
-__device__ __forceinline__ void reduce_tail(const CgArgs& a, int slot, double (&v)[K], double* s_red, Final&& fin) {
+__device__ __forceinline__ bool reduce_tail(const CgArgs& a, int slot, double (&v)[K], double* s_red, Final&& fin) {
     __shared__ int s_last;
     double* part = a.partials + static_cast<size_t>(slot) * a.blocks * kMaxReduce;
     if (threadIdx.x == 0) {
@@ -141,7 +145,7 @@ __device__ __forceinline__ void reduce_tail(const CgArgs& a, int slot, double (&
         s_last = t == gridDim.x - 1;
     }
     __syncthreads();
-    if (!s_last) return;
+    if (!s_last) return false;
     __threadfence();
     double acc[K];
 #pragma unroll
@@ -155,14 +159,15 @@ __device__ __forceinline__ void reduce_tail(const CgArgs& a, int slot, double (&
         a.st->count[slot] = 0;
         fin(acc);
     }
+    return true;
 }
 
 // FP64 per-thread values: FP64 warp and block sums.
 template <int K, typename Final>
-__device__ __forceinline__ void reduce_last(const CgArgs& a, int slot, double (&v)[K], Final&& fin) {
+__device__ __forceinline__ bool reduce_last(const CgArgs& a, int slot, double (&v)[K], Final&& fin) {
     __shared__ double s_red[32 * kMaxReduce];
     block_sum<K>(v, s_red);
-    reduce_tail<K>(a, slot, v, s_red, fin);
+    return reduce_tail<K>(a, slot, v, s_red, fin);
 }
 
 // An unevaluated FP32 pair (hi + lo) for the dot products of the FP32 loop: each
@@ -188,7 +193,7 @@ struct FloatPair {
 // FP32-pair per-thread values (the mixed inner loop): warp sums as pairs, the
 // warps' sums added in FP64 by thread 0.
 template <int K, typename Final>
-__device__ __forceinline__ void reduce_last(const CgArgs& a, int slot, FloatPair (&v)[K], Final&& fin) {
+__device__ __forceinline__ bool reduce_last(const CgArgs& a, int slot, FloatPair (&v)[K], Final&& fin) {
     __shared__ double s_red[32 * kMaxReduce];
     __shared__ float2 s_warp[32 * kMaxReduce];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -230,7 +235,7 @@ __device__ __forceinline__ void reduce_last(const CgArgs& a, int slot, FloatPair
             d[k] = static_cast<double>(w.hi) + static_cast<double>(w.lo);
         }
     }
-    reduce_tail<K>(a, slot, d, s_red, fin);
+    return reduce_tail<K>(a, slot, d, s_red, fin);
 }
 
 // Warp-uniform loop over row groups of 8 (quarter warp per row) across the grid.
@@ -611,12 +616,26 @@ constexpr bool applied_separately() {
     return PRECOND == LFGPU_PRECOND_SUBDOMAIN || PRECOND == LFGPU_PRECOND_IC0;
 }
 
+// With the pointwise preconditioners (Jacobi, 2x2 nodal blocks) mx_update also
+// forms the next direction: its CTAs, all resident (a cooperative launch), wait
+// for the last one to set beta and then rewrite p = z + beta p for their own nodes,
+// with r, p and the preconditioner read again from L2.  The product then gathers
+// p alone, 8 bytes a node instead of the (z, p_old) pair's 16, and writes no p.
+// The values are those of forming p inside the product (the same fma, once per
+// node instead of once per gather), so the iterates do not change.  The separately
+// applied preconditioners keep the (z, p_old) form: their z arrives after mx_update.
+template <int PRECOND>
+constexpr bool direction_in_update() {
+    return !applied_separately<PRECOND>();
+}
+
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
     constexpr bool kSub = applied_separately<PRECOND>();
     double v[2] = {0.0, 0.0};
     const double2* f2 = reinterpret_cast<const double2*>(a.f);
     float4* zp = reinterpret_cast<float4*>(a.zp0);
+    float2* p2 = reinterpret_cast<float2*>(a.p32);
     GRID_NODES(i) {
         const double2 fv = f2[i];
         const float2 rv = make_float2(static_cast<float>(fv.x), static_cast<float>(fv.y));
@@ -627,7 +646,10 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
         reinterpret_cast<float2*>(a.xlo)[i] = make_float2(0.f, 0.f);
         reinterpret_cast<double2*>(a.r64)[i] = fv;
         reinterpret_cast<float2*>(a.r32)[i] = rv;
-        zp[i] = make_float4(zv.x, 0.f, zv.y, 0.f);
+        if constexpr (direction_in_update<PRECOND>())
+            p2[i] = make_float2(pnew(zv.x, 0.f, 0.f), pnew(zv.y, 0.f, 0.f));  // beta = 0, p_old = 0
+        else
+            zp[i] = make_float4(zv.x, 0.f, zv.y, 0.f);
         v[0] += fv.x * fv.x + fv.y * fv.y;
         v[1] += static_cast<double>(rv.x * zv.x + rv.y * zv.y);
     }
@@ -650,8 +672,10 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
     });
 }
 
-// q = K32 p with p = z + beta p_old formed on the fly; each row writes its p.
-template <int STORAGE>
+// q = K32 p and p.q.  DIRECT: p as mx_update left it, gathered alone.  Otherwise
+// p = z + beta p_old is formed on the fly from the (z, p_old) pairs and each row
+// writes its p.
+template <int STORAGE, bool DIRECT>
 __global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
     if (a.st->done) return;
     const float beta = a.st->beta32;
@@ -659,33 +683,53 @@ __global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
     FloatPair acc;
     if (STORAGE == LFGPU_STORAGE_CSR) {
         const float2* zp2 = reinterpret_cast<const float2*>(zp4);
+        const float* p = a.p32;
         csr32_rows(a,
                    [&](int c) {
-                       const float2 v = zp2[c];
-                       return pnew(v.x, v.y, beta);
+                       if constexpr (DIRECT) {
+                           return p[c];
+                       } else {
+                           const float2 v = zp2[c];
+                           return pnew(v.x, v.y, beta);
+                       }
                    },
                    [&](int row, float off) {
-                       const float2 v = zp2[row];
-                       const float pn = pnew(v.x, v.y, beta);
+                       float pn;
+                       if constexpr (DIRECT) {
+                           pn = p[row];
+                       } else {
+                           const float2 v = zp2[row];
+                           pn = pnew(v.x, v.y, beta);
+                           a.p32[row] = pn;
+                       }
                        const float y = with_diag(off, a.dhi[row], a.dlo[row], pn);
-                       a.p32[row] = pn;
                        a.q32[row] = y;
                        acc.add(pn * y);
                    });
     } else {
         const float2* hi2 = reinterpret_cast<const float2*>(a.dhi);
         const float2* lo2 = reinterpret_cast<const float2*>(a.dlo);
+        const float2* p2 = reinterpret_cast<const float2*>(a.p32);
         bsr32_rows(a,
                    [&](int c) {
-                       const float4 v = zp4[c];
-                       return make_float2(pnew(v.x, v.y, beta), pnew(v.z, v.w, beta));
+                       if constexpr (DIRECT) {
+                           return p2[c];
+                       } else {
+                           const float4 v = zp4[c];
+                           return make_float2(pnew(v.x, v.y, beta), pnew(v.z, v.w, beta));
+                       }
                    },
                    [&](int node, float2 off) {
-                       const float4 v = zp4[node];
-                       const float2 pn = make_float2(pnew(v.x, v.y, beta), pnew(v.z, v.w, beta));
+                       float2 pn;
+                       if constexpr (DIRECT) {
+                           pn = p2[node];
+                       } else {
+                           const float4 v = zp4[node];
+                           pn = make_float2(pnew(v.x, v.y, beta), pnew(v.z, v.w, beta));
+                           reinterpret_cast<float2*>(a.p32)[node] = pn;
+                       }
                        const float2 h = hi2[node], l = lo2[node];
                        const float2 y = make_float2(with_diag(off.x, h.x, l.x, pn.x), with_diag(off.y, h.y, l.y, pn.y));
-                       reinterpret_cast<float2*>(a.p32)[node] = pn;
                        reinterpret_cast<float2*>(a.q32)[node] = y;
                        acc.add(pn.x * y.x + pn.y * y.y);
                    });
@@ -705,14 +749,25 @@ __global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
     });
 }
 
-// x += alpha p (into the FP32 pair), r -= alpha q, z = M^-1 r; r.r and r.z.
+__device__ __forceinline__ unsigned ld_acquire_gpu_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// x += alpha p (into the FP32 pair), r -= alpha q, z = M^-1 r; r.r and r.z; with
+// the pointwise preconditioners then p = z + beta p (direction_in_update).
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
     constexpr bool kSub = applied_separately<PRECOND>();
+    constexpr bool kDirect = direction_in_update<PRECOND>();
+    __shared__ int s_go;
     if (a.st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_branch(a, false);
         return;
     }
+    // The flag's value before any CTA arrives: it moves only after all have.
+    const unsigned go0 = kDirect ? a.st->go : 0u;
     const float alpha = a.st->alpha32, alpha_lo = a.st->alpha32_lo;
     const float2* p2 = reinterpret_cast<const float2*>(a.p32);
     const float2* q2 = reinterpret_cast<const float2*>(a.q32);
@@ -734,12 +789,12 @@ __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
         hi2[i] = hv;
         lo2[i] = lv;
         r2[i] = rv;
-        zp_next[i] = make_float4(zv.x, pv.x, zv.y, pv.y);
+        if constexpr (!kDirect) zp_next[i] = make_float4(zv.x, pv.x, zv.y, pv.y);
         rr.add(rv.x * rv.x + rv.y * rv.y);
         if constexpr (!kSub) rz.add(rv.x * zv.x + rv.y * zv.y);
     }
     FloatPair v[2] = {rr, rz};
-    reduce_last<2>(a, 2, v, [&](const double* t) {
+    const bool last = reduce_last<2>(a, 2, v, [&](const double* t) {
         CgState* s = a.st;
         s->it += 1;
         const double rn = sqrt(fmax(0.0, t[0]));
@@ -760,6 +815,53 @@ __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
         set_branch(a, refine && !s->done);
         set_loop(a, !s->done);
     });
+    if constexpr (kDirect) {
+        // Grid-wide wait for beta (bounded).  A CTA whose wait runs out ends the solve.
+        if (threadIdx.x == 0) {
+            int ok = 1;
+            if (last) {
+                asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&a.st->go) : "memory");
+            } else {
+                // The wait lasts about one pass of the update; each poll is an L2
+                // round trip, so the limit is checked on every one.
+                const unsigned long long t0 = global_ns();
+                while (ld_acquire_gpu_u32(&a.st->go) == go0) {
+                    if (wait_expired(a.status, t0, static_cast<int>(blockIdx.x))) {
+                        ok = 0;
+                        break;
+                    }
+                }
+            }
+            if (!ok) {
+                a.st->done = 1;
+                set_branch(a, false);
+                set_loop(a, false);
+            }
+            s_go = ok && !__ldcg(&a.st->done) && !__ldcg(&a.st->refine);
+        }
+        __syncthreads();
+        if (!s_go) return;
+        const float beta = __ldcg(&a.st->beta32);
+        float2* pw = reinterpret_cast<float2*>(a.p32);
+        GRID_NODES(i) {  // this thread's nodes of the pass above
+            const float2 zv = precond32<PRECOND>(a, i, r2[i]);
+            const float2 pv = pw[i];
+            pw[i] = make_float2(pnew(zv.x, pv.x, beta), pnew(zv.y, pv.y, beta));
+        }
+    }
+}
+
+// After a residual replacement with a pointwise preconditioner: p = z + beta p, with
+// the z and beta of mx_reprecondition.
+__global__ void __launch_bounds__(kThreads) mx_direction(CgArgs a) {
+    if (a.st->done || !a.st->refine) return;
+    const float beta = a.st->beta32;
+    const float2* z2 = reinterpret_cast<const float2*>(a.zp0);
+    float2* pw = reinterpret_cast<float2*>(a.p32);
+    GRID_NODES(i) {
+        const float2 zv = z2[i], pv = pw[i];
+        pw[i] = make_float2(pnew(zv.x, pv.x, beta), pnew(zv.y, pv.y, beta));
+    }
 }
 
 // x64 += hi + lo, then hi = lo = 0 (hi + lo is exact in FP64).  Inside the loop it
@@ -826,6 +928,9 @@ __global__ void __launch_bounds__(kThreads) mx_residual(CgArgs a) {
     });
 }
 
+// z = M^-1 r32 after a residual replacement, and beta.  The next direction is
+// formed by the product from the (z, p_old) pairs, or (direction_in_update) by
+// mx_direction from z, kept in the first half of zp0.
 template <int PRECOND>
 __global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
     if (a.st->done || !a.st->refine) return;
@@ -835,10 +940,14 @@ __global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
     GRID_NODES(i) {
         const float2 rv = r2[i];
         const float2 zv = precond32<PRECOND>(a, i, rv);
-        float4 t = zp[i];
-        t.x = zv.x;
-        t.z = zv.y;
-        zp[i] = t;
+        if constexpr (direction_in_update<PRECOND>()) {
+            reinterpret_cast<float2*>(a.zp0)[i] = zv;
+        } else {
+            float4 t = zp[i];
+            t.x = zv.x;
+            t.z = zv.y;
+            zp[i] = t;
+        }
         rz.add(rv.x * zv.x + rv.y * zv.y);
     }
     FloatPair v[1] = {rz};
@@ -1535,7 +1644,7 @@ struct GraphBuilder {
 
 template <typename K>
 void add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep, int ndep, K kernel, int blocks,
-                CgArgs* args, int smem = 0, int threads = kThreads) {
+                CgArgs* args, int smem = 0, int threads = kThreads, bool cooperative = false) {
     cudaKernelNodeParams p = {};
     p.func = reinterpret_cast<void*>(kernel);
     p.gridDim = dim3(blocks);
@@ -1544,6 +1653,22 @@ void add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep
     void* params[1] = {args};
     p.kernelParams = params;
     LF_CUDA(cudaGraphAddKernelNode(node, g, dep, ndep, &p));
+    if (cooperative) {  // every CTA resident at once, or the launch fails
+        cudaLaunchAttributeValue v = {};
+        v.cooperative = 1;
+        LF_CUDA(cudaGraphKernelNodeSetAttribute(*node, cudaLaunchAttributeCooperative, &v));
+    }
+}
+
+// CTAs of a kernel that waits on a grid-wide flag: at most `want`, and no more than
+// the device keeps resident at once.
+template <typename K>
+int resident_grid(K kernel, int want) {
+    int dev = 0, sms = 0, per_sm = 0;
+    LF_CUDA(cudaGetDevice(&dev));
+    LF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    LF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0));
+    return std::max(1, std::min(want, per_sm * sms));
 }
 
 cudaGraphNode_t add_conditional(cudaGraph_t g, const cudaGraphNode_t* dep, int ndep, cudaGraphConditionalHandle h,
@@ -1600,6 +1725,8 @@ cudaGraphNode_t add_mixed_apply(cudaGraph_t g, cudaGraphNode_t dep, CgArgs* a, i
 template <int STORAGE, int PRECOND>
 void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub_threads = 0, int smem = 0) {
     constexpr bool kSub = applied_separately<PRECOND>();
+    constexpr bool kDirect = direction_in_update<PRECOND>();
+    const int update_grid = kDirect ? resident_grid(mx_update<PRECOND>, blocks) : blocks;
     cudaGraphNode_t n_init;
     add_kernel(g, &n_init, nullptr, 0, mx_init<PRECOND>, blocks, a);
     if constexpr (kSub) n_init = add_mixed_apply<PRECOND>(g, n_init, a, sub_grid, sub_threads, smem);
@@ -1617,9 +1744,9 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub
         halves[h] = *a;
         CgArgs* ah = &halves[h];
         LF_CUDA(cudaGraphConditionalHandleCreate(&ah->branch, body, 0, 0));
-        cudaGraphNode_t k1, k2, k3, k4, k5;
-        add_kernel(body, &k1, prev ? &prev : nullptr, prev ? 1 : 0, mx_product<STORAGE>, blocks, ah);
-        add_kernel(body, &k2, &k1, 1, mx_update<PRECOND>, blocks, ah);
+        cudaGraphNode_t k1, k2, k3, k4, k5, k6;
+        add_kernel(body, &k1, prev ? &prev : nullptr, prev ? 1 : 0, mx_product<STORAGE, kDirect>, blocks, ah);
+        add_kernel(body, &k2, &k1, 1, mx_update<PRECOND>, update_grid, ah, 0, kThreads, kDirect);
         cudaGraph_t branch;
         prev = add_conditional(body, &k2, 1, ah->branch, cudaGraphCondTypeIf, &branch);
         add_kernel(branch, &k3, nullptr, 0, mx_flush<false>, blocks, ah);
@@ -1628,6 +1755,7 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub
             prev = add_mixed_apply<PRECOND>(body, prev, ah, sub_grid, sub_threads, smem);
         } else {
             add_kernel(branch, &k5, &k4, 1, mx_reprecondition<PRECOND>, blocks, ah);
+            add_kernel(branch, &k6, &k5, 1, mx_direction, blocks, ah);
         }
     }
 }
@@ -1691,18 +1819,34 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
         LF_CUDA(cudaGetLastError());
         trail.mark(phase);
     };
+    constexpr bool kDirect = direction_in_update<PRECOND>();
+    auto update = [&](int phase) {
+        if constexpr (kDirect) {  // its CTAs wait for one another: a cooperative launch
+            void* args[1] = {a};
+            LF_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(mx_update<PRECOND>),
+                                                dim3(resident_grid(mx_update<PRECOND>, blocks)), dim3(kThreads), args,
+                                                0, stream));
+            trail.mark(phase);
+        } else {
+            chain(mx_update<PRECOND>, phase);
+        }
+    };
     if (!mixed && a->x0) chain(cg64_residual<STORAGE>, -1);
     if (mixed) chain(mx_init<PRECOND>, -1);
     else if constexpr (!kSub) chain(cg64_init<PRECOND>, -1);
     if (kSub) sub_apply(-1);
     for (int k = 0; k < iters; ++k) {
         if (mixed) {
-            chain(mx_product<STORAGE>, 0);
-            chain(mx_update<PRECOND>, 1);
+            chain(mx_product<STORAGE, kDirect>, 0);
+            update(1);
             chain(mx_flush<false>, 2);
             chain(mx_residual<STORAGE>, 2);
-            if constexpr (kSub) sub_apply(3);
-            else chain(mx_reprecondition<PRECOND>, 3);
+            if constexpr (kSub) {
+                sub_apply(3);
+            } else {
+                chain(mx_reprecondition<PRECOND>, 3);
+                chain(mx_direction, 3);
+            }
         } else if constexpr (!kSub) {  // the FP64 subdomain form is launch_separate_unrolled
             chain(cg64_product<STORAGE>, 0);
             chain(cg64_update<PRECOND>, 1);
@@ -2045,13 +2189,13 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
                                                 2 * st.refs) +
                       1;
     else if (s.unrolled > 0)
-        c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 5 : 3) +
+        c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 6 : 3) +
                       (s.mixed ? 1 : 0);
-    else  // mixed: kBodyIterations iterations (two kernels each) a pass, the branch's flush, residual and
-          // re-preconditioning per replacement, a final flush after the loop
+    else  // mixed: kBodyIterations iterations (two kernels each) a pass, the branch's flush, residual,
+          // re-preconditioning and direction per replacement, a final flush after the loop
         c.launches += (s.x0 ? 1 : 0) + 1 +
                       (s.mixed ? 2 * kBodyIterations * ((st.it + kBodyIterations - 1) / kBodyIterations) +
-                                     3 * st.refs + 1
+                                     4 * st.refs + 1
                                : 3 * st.it);
     PcgResult r{};
     r.iterations = st.it;
