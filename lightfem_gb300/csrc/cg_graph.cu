@@ -580,10 +580,11 @@ __global__ void __launch_bounds__(kThreads) cg64_direction(CgArgs a) {
 }
 
 // ------------------------------------------------------------------ mixed kernels
-// FP32 vectors of the inner solve.  z and p are interleaved per DOF, (z_c, p_c),
-// so the product gathers both with one 16-byte load per node; two copies
-// alternate between iterations (the product reads one, the update writes the
-// other).  The solution correction since the last residual replacement is kept
+// FP32 vectors of the inner solve.  With the pointwise preconditioners p is a
+// plain vector that mx_update rewrites (direction_in_update).  With the separately
+// applied ones z and p are interleaved per DOF, (z_c, p_c), so the product gathers
+// both with one 16-byte load per node and forms p; two copies alternate between
+// iterations (the product reads one, the update writes the other).  The solution correction since the last residual replacement is kept
 // as an unevaluated FP32 pair (hi + lo, about 48 significant bits) and added to
 // the FP64 solution when a replacement is due, so no FP64 arithmetic runs per
 // iteration.
@@ -758,9 +759,15 @@ __device__ __forceinline__ unsigned ld_acquire_gpu_u32(const unsigned* p) {
 // x += alpha p (into the FP32 pair), r -= alpha q, z = M^-1 r; r.r and r.z; with
 // the pointwise preconditioners then p = z + beta p (direction_in_update).
 template <int PRECOND>
-__global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
+__global__ void __launch_bounds__(kThreads, 8) mx_update(CgArgs a) {  // 8 CTAs an SM: all 1,216 resident
     constexpr bool kSub = applied_separately<PRECOND>();
     constexpr bool kDirect = direction_in_update<PRECOND>();
+    // Jacobi: the second pass takes (z, p) of this thread's first kStash nodes from
+    // here (four cover 1,002,001 nodes on 1,216 CTAs of 256 threads) and reads r, p
+    // and the inverse diagonal of any further ones again.  The 2x2 blocks read all
+    // again: their update does not fit 32 registers with the stash.
+    constexpr int kStash = (kDirect && PRECOND == LFGPU_PRECOND_JACOBI) ? 4 : 0;
+    __shared__ float4 s_zp[kStash > 0 ? kStash : 1][kThreads];
     __shared__ int s_go;
     if (a.st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_branch(a, false);
@@ -776,6 +783,7 @@ __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
     float2* lo2 = reinterpret_cast<float2*>(a.xlo);
     float4* zp_next = zp_buffer(a, a.st->it + 1);
     FloatPair rr, rz;
+    int k = 0;
     GRID_NODES(i) {
         const float2 pv = p2[i], qv = q2[i];
         float2 hv = hi2[i], lv = lo2[i];
@@ -789,7 +797,12 @@ __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
         hi2[i] = hv;
         lo2[i] = lv;
         r2[i] = rv;
-        if constexpr (!kDirect) zp_next[i] = make_float4(zv.x, pv.x, zv.y, pv.y);
+        if constexpr (kDirect) {
+            if (k < kStash) s_zp[k][threadIdx.x] = make_float4(zv.x, zv.y, pv.x, pv.y);
+            ++k;
+        } else {
+            zp_next[i] = make_float4(zv.x, pv.x, zv.y, pv.y);
+        }
         rr.add(rv.x * rv.x + rv.y * rv.y);
         if constexpr (!kSub) rz.add(rv.x * zv.x + rv.y * zv.y);
     }
@@ -843,9 +856,18 @@ __global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
         if (!s_go) return;
         const float beta = __ldcg(&a.st->beta32);
         float2* pw = reinterpret_cast<float2*>(a.p32);
+        k = 0;
         GRID_NODES(i) {  // this thread's nodes of the pass above
-            const float2 zv = precond32<PRECOND>(a, i, r2[i]);
-            const float2 pv = pw[i];
+            float2 zv, pv;
+            if (k < kStash) {
+                const float4 t = s_zp[k][threadIdx.x];
+                zv = make_float2(t.x, t.y);
+                pv = make_float2(t.z, t.w);
+            } else {
+                zv = precond32<PRECOND>(a, i, r2[i]);
+                pv = pw[i];
+            }
+            ++k;
             pw[i] = make_float2(pnew(zv.x, pv.x, beta), pnew(zv.y, pv.y, beta));
         }
     }
@@ -1409,13 +1431,23 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
     }
     if (!ok) s_failed = 1;
     __syncthreads();
+    // No CTA leaves while a cluster peer is still in its level loop, where it
+    // stores into this CTA's ring.  Every CTA gets here: each of its waits is bounded.
+    cluster_sync_all();
     if (s_failed) {
-        // A wait ran out: end the solve (the status word already says why).
+        // A wait ran out: end the solve (the status word already says why).  Peers'
+        // results issued before the barrier may still be landing in the ring, whose
+        // phases this CTA no longer tracks: it stays 100 us before it releases its
+        // shared memory.
         if (tid == 0) {
             a.st->status = LFGPU_ERR_TIMEOUT;
             a.st->done = 1;
             set_loop(a, false);
+            const unsigned long long t0 = global_ns();
+            while (global_ns() - t0 < 100000ull) {
+            }
         }
+        __syncthreads();
         return;
     }
     if constexpr (MODE == 3) {
@@ -2168,8 +2200,7 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     // IC(0): residual (warm start), init, two sweeps and start, then six kernels a
     // pass; subdomain block-Jacobi: one apply kernel in place of the two sweeps.
     // IC(0) by levels: a gather of r (ic0_sweep_inputs) before the two sweeps.
-    const bool levels = c.ic0_sweep != LFGPU_IC0_SWEEP_POLLED && c.sweep_window > 0 &&
-                        c.sweep_pattern_version == c.pattern_version;
+    const bool levels = c.ic0_sweep != LFGPU_IC0_SWEEP_POLLED && ic0_levels_chosen(c, s.mixed);
     if (s.precond == LFGPU_PRECOND_IC0 && s.mixed)  // mixed: init, gather and two sweeps, then product, update,
                                                     // gather and two sweeps an iteration, flush and residual per
                                                     // replacement, final flush

@@ -344,12 +344,27 @@ void ensure_ic0_sweep_values(Context& c, bool fp32) {
     LF_CUDA(cudaGetLastError());
 }
 
+// LFGPU_IC0_SWEEP_AUTO takes the FP64 level sweeps where the forward schedule's
+// levels hold kLevelsMinWidth rows on average or more.  A level costs them about
+// 1.8 us whatever its width (one row's FP64 chain plus the exchange); the polled
+// sweeps' cost per level grows with it.  Per forward + backward application on
+// GB300 (cantilever workloads, RCM): 200x200, 50 rows a level: polled 3.9 ms,
+// levels 5.6 ms; 500x500, 125 rows: 13.3-13.6 ms, 14.1 ms; 1000x1000, 250 rows:
+// 30.5-30.9 ms, 28.4 ms.
+constexpr i64 kLevelsMinWidth = 192;
+
+bool ic0_levels_chosen(const Context& c, bool required) {
+    if (c.sweep_window <= 0 || c.sweep_pattern_version != c.pattern_version) return false;
+    if (required || c.ic0_sweep == LFGPU_IC0_SWEEP_LEVELS) return true;
+    return c.ic0_sweep == LFGPU_IC0_SWEEP_AUTO && c.n >= kLevelsMinWidth * c.sweep[0].levels;
+}
+
 bool ic0_use_levels(Context& c, bool required) {
     if (c.ic0_sweep == LFGPU_IC0_SWEEP_POLLED && !required) return false;
     LF_REQUIRE(c.ic0_sweep != LFGPU_IC0_SWEEP_POLLED, LFGPU_ERR_UNSUPPORTED,
                "mixed-precision ic0 needs the level-scheduled sweeps");
     ensure_ic0_schedule(c);
-    if (c.sweep_window > 0) return true;
+    if (c.sweep_window > 0) return ic0_levels_chosen(c, required);
     LF_REQUIRE(!required && c.ic0_sweep == LFGPU_IC0_SWEEP_AUTO, LFGPU_ERR_UNSUPPORTED,
                "the ic0 level schedule does not fit the sweep's shared-memory ring");
     return false;

@@ -74,9 +74,13 @@ void ensure_ic0_schedule(Context& c);
 // The factor in schedule order for the level sweeps, per K version: FP64, and the
 // FP32 copy when fp32 is set.  Requires ensure_ic0 and ensure_ic0_schedule.
 void ensure_ic0_sweep_values(Context& c, bool fp32);
-// Whether the level-scheduled sweeps run for this handle (option and schedule fit);
-// throws LFGPU_ERR_UNSUPPORTED when they are required but the schedule does not fit.
+// Whether the level-scheduled sweeps run for this handle (option, schedule fit and,
+// for LFGPU_IC0_SWEEP_AUTO, the average level width; `required`: the mixed loop,
+// which has no other FP32 sweeps); throws LFGPU_ERR_UNSUPPORTED when they are
+// required but the schedule does not fit.
 bool ic0_use_levels(Context& c, bool required);
+// The same choice for a schedule already built (no side effects).
+bool ic0_levels_chosen(const Context& c, bool required);
 
 // The level-scheduled sweeps run as one cluster of kSweepCluster CTAs of
 // kSweepThreads consumer threads and a producer warp; every CTA keeps a ring of

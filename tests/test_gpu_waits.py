@@ -10,6 +10,12 @@ option (LFGPU_OPTION_WAIT_LIMIT_NS, 4 s by default); here it is set to 1 ns, so
 the first wait that has to spin at all runs out.  Nothing is faulted, trapped or
 hung: the waits end on their own limit, on waits the kernels make in every solve.
 
+The level sweeps' waits are not made to run out here.  A CTA of the sweep's
+cluster that gave up no longer knows which of its peers' stores into its shared
+memory are still in flight; it waits for its peers at a cluster barrier and then
+a grace period before it exits, which bounds the path but does not prove it safe,
+so it is not exercised on a shared GPU.
+
 The reference has no device waits; a solve that ends this way maps to the
 runtime_error path of src/main.cpp:162-164 like its other PCG failures
 (src/solver.cpp:579-593).
