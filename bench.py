@@ -555,6 +555,7 @@ def run_ours(args) -> int:
         precision = args.profile_precision or ("fp64" if args.precond in ("ic0", "subdomain") else "mixed")
         if args.precond == "subdomain":
             ctx.set_subdomains(args.subdomain_nodes, args.subdomain_split)
+        ctx.set_option(_native.OPTION_IC0_SWEEP, _native.IC0_SWEEP[args.ic0_sweep])
         capped = ctx.options(tol, args.profile_iters, args.storage, args.precond, precision, "reliable")
         ms, rep = step(capped)
         unrolled = ctx.options(tol, 10 ** 6, args.storage, args.precond, precision, "reliable",
@@ -752,6 +753,8 @@ def main() -> int:
     ap.add_argument("--profile-precision", choices=("fp64", "mixed"), default=None,
                     help="precision of the --profile-iters run (default: fp64 for ic0 and subdomain, else mixed)")
     ap.add_argument("--subdomain-split", choices=("rcb", "chunk"), default="rcb")
+    ap.add_argument("--ic0-sweep", choices=("auto", "levels", "polled"), default="auto",
+                    help="IC(0) sweeps of the --profile-iters run (auto: levels where the average level is wide)")
     ap.add_argument("--scale", type=int, default=1, help="divide the mesh size (testing only)")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=3)
