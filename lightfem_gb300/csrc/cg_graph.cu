@@ -580,9 +580,8 @@ __global__ void __launch_bounds__(kThreads) cg64_direction(CgArgs a) {
 }
 
 // ------------------------------------------------------------------ mixed kernels
-// FP32 vectors of the inner solve.  With the pointwise preconditioners p is a
-// plain vector that mx_update rewrites (direction_in_update).  With the separately
-// applied ones z and p are interleaved per DOF, (z_c, p_c), so the product gathers
+// FP32 vectors of the inner solve.  In the direct form (see kDirectMinNodes) p is
+// a plain vector that mx_update rewrites.  Otherwise z and p are interleaved per DOF, (z_c, p_c), so the product gathers
 // both with one 16-byte load per node and forms p; two copies alternate between
 // iterations (the product reads one, the update writes the other).  The solution correction since the last residual replacement is kept
 // as an unevaluated FP32 pair (hi + lo, about 48 significant bits) and added to
@@ -617,22 +616,30 @@ constexpr bool applied_separately() {
     return PRECOND == LFGPU_PRECOND_SUBDOMAIN || PRECOND == LFGPU_PRECOND_IC0;
 }
 
-// With the pointwise preconditioners (Jacobi, 2x2 nodal blocks) mx_update also
-// forms the next direction: its CTAs, all resident (a cooperative launch), wait
-// for the last one to set beta and then rewrite p = z + beta p for their own nodes,
-// with r, p and the preconditioner read again from L2.  The product then gathers
-// p alone, 8 bytes a node instead of the (z, p_old) pair's 16, and writes no p.
-// The values are those of forming p inside the product (the same fma, once per
-// node instead of once per gather), so the iterates do not change.  The separately
-// applied preconditioners keep the (z, p_old) form: their z arrives after mx_update.
-template <int PRECOND>
-constexpr bool direction_in_update() {
-    return !applied_separately<PRECOND>();
+// DIRECT form, with the pointwise preconditioners (Jacobi, 2x2 nodal blocks) on
+// meshes of kDirectMinNodes nodes or more: mx_update also forms the next
+// direction.  Its CTAs, all resident (a cooperative launch), wait for the last one
+// to set beta and then rewrite p = z + beta p for their own nodes.  The product
+// then gathers p alone, 8 bytes a node instead of the (z, p_old) pair's 16, and
+// writes no p.  The values are those of forming p inside the product (the same
+// fma, once per node instead of once per gather), so the iterates do not change.
+// The wait costs a few microseconds whatever the size, the saving grows with it.
+// Per iteration of the mixed BSR/Jacobi solve on GB300 (n x n plane-strain
+// cantilevers, RCM), direct against (z, p_old) form: 400x400 (160,801 nodes)
+// 29.9 against 27.6 us; 600x600 (361,201) 39.6 against 36.1; 700x700 (491,401)
+// 43.3 against 42.2; 800x800 (641,601) 50.0 against 51.0; 1000x1000 (1,002,001)
+// 63.6 against 73.7.  The separately applied preconditioners keep the (z, p_old)
+// form: their z arrives after mx_update.
+constexpr long long kDirectMinNodes = 576000;
+
+bool direct_form(int precond, long long nodes) {
+    return (precond == LFGPU_PRECOND_JACOBI || precond == LFGPU_PRECOND_BLOCK2) && nodes >= kDirectMinNodes;
 }
 
-template <int PRECOND>
+template <int PRECOND, bool DIRECT>
 __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
     constexpr bool kSub = applied_separately<PRECOND>();
+    static_assert(!(DIRECT && kSub), "the direct form needs a pointwise preconditioner");
     double v[2] = {0.0, 0.0};
     const double2* f2 = reinterpret_cast<const double2*>(a.f);
     float4* zp = reinterpret_cast<float4*>(a.zp0);
@@ -647,7 +654,7 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
         reinterpret_cast<float2*>(a.xlo)[i] = make_float2(0.f, 0.f);
         reinterpret_cast<double2*>(a.r64)[i] = fv;
         reinterpret_cast<float2*>(a.r32)[i] = rv;
-        if constexpr (direction_in_update<PRECOND>())
+        if constexpr (DIRECT)
             p2[i] = make_float2(pnew(zv.x, 0.f, 0.f), pnew(zv.y, 0.f, 0.f));  // beta = 0, p_old = 0
         else
             zp[i] = make_float4(zv.x, 0.f, zv.y, 0.f);
@@ -757,11 +764,12 @@ __device__ __forceinline__ unsigned ld_acquire_gpu_u32(const unsigned* p) {
 }
 
 // x += alpha p (into the FP32 pair), r -= alpha q, z = M^-1 r; r.r and r.z; with
-// the pointwise preconditioners then p = z + beta p (direction_in_update).
-template <int PRECOND>
+// the direct form then p = z + beta p.
+template <int PRECOND, bool DIRECT>
 __global__ void __launch_bounds__(kThreads, 8) mx_update(CgArgs a) {  // 8 CTAs an SM: all 1,216 resident
     constexpr bool kSub = applied_separately<PRECOND>();
-    constexpr bool kDirect = direction_in_update<PRECOND>();
+    constexpr bool kDirect = DIRECT;
+    static_assert(!(DIRECT && kSub), "the direct form needs a pointwise preconditioner");
     // Jacobi: the second pass takes (z, p) of this thread's first kStash nodes from
     // here (four cover 1,002,001 nodes on 1,216 CTAs of 256 threads) and reads r, p
     // and the inverse diagonal of any further ones again.  The 2x2 blocks read all
@@ -951,9 +959,9 @@ __global__ void __launch_bounds__(kThreads) mx_residual(CgArgs a) {
 }
 
 // z = M^-1 r32 after a residual replacement, and beta.  The next direction is
-// formed by the product from the (z, p_old) pairs, or (direction_in_update) by
-// mx_direction from z, kept in the first half of zp0.
-template <int PRECOND>
+// formed by the product from the (z, p_old) pairs, or (DIRECT) by mx_direction
+// from z, kept in the first half of zp0.
+template <int PRECOND, bool DIRECT>
 __global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
     if (a.st->done || !a.st->refine) return;
     const float2* r2 = reinterpret_cast<const float2*>(a.r32);
@@ -962,7 +970,7 @@ __global__ void __launch_bounds__(kThreads) mx_reprecondition(CgArgs a) {
     GRID_NODES(i) {
         const float2 rv = r2[i];
         const float2 zv = precond32<PRECOND>(a, i, rv);
-        if constexpr (direction_in_update<PRECOND>()) {
+        if constexpr (DIRECT) {
             reinterpret_cast<float2*>(a.zp0)[i] = zv;
         } else {
             float4 t = zp[i];
@@ -1754,13 +1762,13 @@ cudaGraphNode_t add_mixed_apply(cudaGraph_t g, cudaGraphNode_t dep, CgArgs* a, i
 // Preconditioners applied by their own kernels add them after mx_init and after
 // each iteration's IF node; the branch then holds only the flush and the FP64
 // residual, as the kernels after it re-precondition.
-template <int STORAGE, int PRECOND>
+template <int STORAGE, int PRECOND, bool DIRECT>
 void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub_threads = 0, int smem = 0) {
     constexpr bool kSub = applied_separately<PRECOND>();
-    constexpr bool kDirect = direction_in_update<PRECOND>();
-    const int update_grid = kDirect ? resident_grid(mx_update<PRECOND>, blocks) : blocks;
+    constexpr bool kDirect = DIRECT;
+    const int update_grid = kDirect ? resident_grid(mx_update<PRECOND, DIRECT>, blocks) : blocks;
     cudaGraphNode_t n_init;
-    add_kernel(g, &n_init, nullptr, 0, mx_init<PRECOND>, blocks, a);
+    add_kernel(g, &n_init, nullptr, 0, mx_init<PRECOND, DIRECT>, blocks, a);
     if constexpr (kSub) n_init = add_mixed_apply<PRECOND>(g, n_init, a, sub_grid, sub_threads, smem);
     cudaGraph_t body;
     const cudaGraphNode_t n_loop = add_conditional(g, &n_init, 1, a->loop, cudaGraphCondTypeWhile, &body);
@@ -1778,7 +1786,7 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub
         LF_CUDA(cudaGraphConditionalHandleCreate(&ah->branch, body, 0, 0));
         cudaGraphNode_t k1, k2, k3, k4, k5, k6;
         add_kernel(body, &k1, prev ? &prev : nullptr, prev ? 1 : 0, mx_product<STORAGE, kDirect>, blocks, ah);
-        add_kernel(body, &k2, &k1, 1, mx_update<PRECOND>, update_grid, ah, 0, kThreads, kDirect);
+        add_kernel(body, &k2, &k1, 1, mx_update<PRECOND, DIRECT>, update_grid, ah, 0, kThreads, kDirect);
         cudaGraph_t branch;
         prev = add_conditional(body, &k2, 1, ah->branch, cudaGraphCondTypeIf, &branch);
         add_kernel(branch, &k3, nullptr, 0, mx_flush<false>, blocks, ah);
@@ -1786,8 +1794,8 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub
         if constexpr (kSub) {
             prev = add_mixed_apply<PRECOND>(body, prev, ah, sub_grid, sub_threads, smem);
         } else {
-            add_kernel(branch, &k5, &k4, 1, mx_reprecondition<PRECOND>, blocks, ah);
-            add_kernel(branch, &k6, &k5, 1, mx_direction, blocks, ah);
+            add_kernel(branch, &k5, &k4, 1, mx_reprecondition<PRECOND, DIRECT>, blocks, ah);
+            if constexpr (kDirect) add_kernel(branch, &k6, &k5, 1, mx_direction, blocks, ah);
         }
     }
 }
@@ -1828,7 +1836,7 @@ struct EventTrail {
 // is due).  Profilers see these launches; they do not descend into graph nodes.
 // Phase slots: 0 product, 1 update, 2 FP64 p update or mixed residual
 // replacement, 3 mixed re-preconditioning (subdomain: the block solves).
-template <int STORAGE, int PRECOND>
+template <int STORAGE, int PRECOND, bool DIRECT = false>
 void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int iters, EventTrail& trail,
                      int sub_grid = 0, int sub_threads = 0, int smem = 0) {
     constexpr bool kSub = applied_separately<PRECOND>();
@@ -1851,20 +1859,20 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
         LF_CUDA(cudaGetLastError());
         trail.mark(phase);
     };
-    constexpr bool kDirect = direction_in_update<PRECOND>();
+    constexpr bool kDirect = DIRECT;
     auto update = [&](int phase) {
         if constexpr (kDirect) {  // its CTAs wait for one another: a cooperative launch
             void* args[1] = {a};
-            LF_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(mx_update<PRECOND>),
-                                                dim3(resident_grid(mx_update<PRECOND>, blocks)), dim3(kThreads), args,
-                                                0, stream));
+            LF_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(mx_update<PRECOND, DIRECT>),
+                                                dim3(resident_grid(mx_update<PRECOND, DIRECT>, blocks)),
+                                                dim3(kThreads), args, 0, stream));
             trail.mark(phase);
         } else {
-            chain(mx_update<PRECOND>, phase);
+            chain(mx_update<PRECOND, DIRECT>, phase);
         }
     };
     if (!mixed && a->x0) chain(cg64_residual<STORAGE>, -1);
-    if (mixed) chain(mx_init<PRECOND>, -1);
+    if (mixed) chain(mx_init<PRECOND, DIRECT>, -1);
     else if constexpr (!kSub) chain(cg64_init<PRECOND>, -1);
     if (kSub) sub_apply(-1);
     for (int k = 0; k < iters; ++k) {
@@ -1876,8 +1884,8 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
             if constexpr (kSub) {
                 sub_apply(3);
             } else {
-                chain(mx_reprecondition<PRECOND>, 3);
-                chain(mx_direction, 3);
+                chain(mx_reprecondition<PRECOND, DIRECT>, 3);
+                if constexpr (kDirect) chain(mx_direction, 3);
             }
         } else if constexpr (!kSub) {  // the FP64 subdomain form is launch_separate_unrolled
             chain(cg64_product<STORAGE>, 0);
@@ -1886,6 +1894,19 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
         }
     }
     if (mixed) chain(mx_flush<true>, -1);
+}
+
+// The pointwise preconditioners' mixed loop in the direct form or the (z, p_old)
+// form, by mesh size (kDirectMinNodes).
+template <int STORAGE, int PRECOND>
+void build_pointwise(cudaGraph_t g, CgArgs* a, int blocks) {
+    if (direct_form(PRECOND, a->nb)) build_mixed<STORAGE, PRECOND, true>(g, a, blocks);
+    else build_mixed<STORAGE, PRECOND, false>(g, a, blocks);
+}
+template <int STORAGE, int PRECOND>
+void launch_pointwise(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int iters, EventTrail& trail) {
+    if (mixed && direct_form(PRECOND, a->nb)) launch_unrolled<STORAGE, PRECOND, true>(stream, a, blocks, mixed, iters, trail);
+    else launch_unrolled<STORAGE, PRECOND, false>(stream, a, blocks, mixed, iters, trail);
 }
 
 // IC(0): init -> forward -> backward -> start -> WHILE { product ; update ;
@@ -2146,10 +2167,10 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         else if (ic)
             launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_IC0>(c.stream, &a, blocks, mx, s.unrolled, trail, 0, 0,
                                                                   ap.smem);
-        else if (csr && jac) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
-        else if (csr) launch_unrolled<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled, trail);
-        else if (jac) launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
-        else launch_unrolled<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled, trail);
+        else if (csr && jac) launch_pointwise<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
+        else if (csr) launch_pointwise<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled, trail);
+        else if (jac) launch_pointwise<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(c.stream, &a, blocks, mx, s.unrolled, trail);
+        else launch_pointwise<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(c.stream, &a, blocks, mx, s.unrolled, trail);
         LF_CUDA(cudaEventRecord(c.ev_b, c.stream));
         *kernel_ms = elapsed_ms(c);
         PcgResult res = finish_cg(c, s);
@@ -2166,17 +2187,19 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         else build_fp64<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
     } else {
         if (sub && csr)
-            build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_SUBDOMAIN>(gb.graph, &a, blocks, ap.sub_grid, ap.sub_threads);
+            build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_SUBDOMAIN, false>(gb.graph, &a, blocks, ap.sub_grid,
+                                                                          ap.sub_threads);
         else if (sub)
-            build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_SUBDOMAIN>(gb.graph, &a, blocks, ap.sub_grid, ap.sub_threads);
+            build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_SUBDOMAIN, false>(gb.graph, &a, blocks, ap.sub_grid,
+                                                                          ap.sub_threads);
         else if (ic && csr)
-            build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_IC0>(gb.graph, &a, blocks, 0, 0, ap.smem);
+            build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_IC0, false>(gb.graph, &a, blocks, 0, 0, ap.smem);
         else if (ic)
-            build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_IC0>(gb.graph, &a, blocks, 0, 0, ap.smem);
-        else if (csr && jac) build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
-        else if (csr) build_mixed<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
-        else if (jac) build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
-        else build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
+            build_mixed<LFGPU_STORAGE_BSR, LFGPU_PRECOND_IC0, false>(gb.graph, &a, blocks, 0, 0, ap.smem);
+        else if (csr && jac) build_pointwise<LFGPU_STORAGE_CSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
+        else if (csr) build_pointwise<LFGPU_STORAGE_CSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
+        else if (jac) build_pointwise<LFGPU_STORAGE_BSR, LFGPU_PRECOND_JACOBI>(gb.graph, &a, blocks);
+        else build_pointwise<LFGPU_STORAGE_BSR, LFGPU_PRECOND_BLOCK2>(gb.graph, &a, blocks);
     }
     cudaGraphExec_t exec = nullptr;
     LF_CUDA(cudaGraphInstantiate(&exec, gb.graph, 0));
@@ -2201,6 +2224,7 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
     // pass; subdomain block-Jacobi: one apply kernel in place of the two sweeps.
     // IC(0) by levels: a gather of r (ic0_sweep_inputs) before the two sweeps.
     const bool levels = c.ic0_sweep != LFGPU_IC0_SWEEP_POLLED && ic0_levels_chosen(c, s.mixed);
+    const int direct = s.mixed && direct_form(s.precond, c.n / 2) ? 1 : 0;
     if (s.precond == LFGPU_PRECOND_IC0 && s.mixed)  // mixed: init, gather and two sweeps, then product, update,
                                                     // gather and two sweeps an iteration, flush and residual per
                                                     // replacement, final flush
@@ -2220,13 +2244,13 @@ PcgResult finish_cg(Context& c, const SolveSetup& s) {
                                                 2 * st.refs) +
                       1;
     else if (s.unrolled > 0)
-        c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 6 : 3) +
+        c.launches += (s.x0 && !s.mixed ? 1 : 0) + 1 + static_cast<i64>(s.unrolled) * (s.mixed ? 5 + direct : 3) +
                       (s.mixed ? 1 : 0);
     else  // mixed: kBodyIterations iterations (two kernels each) a pass, the branch's flush, residual,
-          // re-preconditioning and direction per replacement, a final flush after the loop
+          // re-preconditioning (and direction, direct form) per replacement, a final flush after the loop
         c.launches += (s.x0 ? 1 : 0) + 1 +
                       (s.mixed ? 2 * kBodyIterations * ((st.it + kBodyIterations - 1) / kBodyIterations) +
-                                     4 * st.refs + 1
+                                     (3 + direct) * st.refs + 1
                                : 3 * st.it);
     PcgResult r{};
     r.iterations = st.it;

@@ -3,9 +3,9 @@ LFGPU_ERR_TIMEOUT instead of hanging, and the handle stays usable.
 
 Every spin-wait of the kernels (the persistent solver's grid barrier, the mixed
 update's wait for beta, the IC(0) sweeps' operand polls, the level sweeps'
-mbarrier waits) gives up after the
-handle's wait limit, records LFGPU_ERR_TIMEOUT, raises the abort flag that ends
-every other wait, and lets its kernel run to the end.  The limit is a handle
+mbarrier waits) gives up after the handle's wait limit, records
+LFGPU_ERR_TIMEOUT, raises the abort flag that ends every other wait, and lets its
+kernel run to the end.  The limit is a handle
 option (LFGPU_OPTION_WAIT_LIMIT_NS, 4 s by default); here it is set to 1 ns, so
 the first wait that has to spin at all runs out.  Nothing is faulted, trapped or
 hung: the waits end on their own limit, on waits the kernels make in every solve.
@@ -84,10 +84,11 @@ def test_persistent_grid_barrier_expires(native, golden_json):
 
 
 def test_mixed_update_direction_wait_expires(native, golden_json):
-    """The mixed loop's update with a pointwise preconditioner: its CTAs wait for
-    the last one's beta before they form the next direction; with a 1 ns limit the
-    first CTA to wait gives up and the solve ends."""
-    model, ctx = _system(native, mesh.workload(1, scale=4))
+    """The mixed loop's update in its direct form (a pointwise preconditioner on a
+    mesh of 576,000 nodes or more): its CTAs wait for the last one's beta before
+    they form the next direction; with a 1 ns limit the first CTA to wait gives up
+    and the solve ends."""
+    model, ctx = _system(native, mesh.workload(2))  # 1000x1000, 1,002,001 nodes
     ctx.set_option(native.OPTION_WAIT_LIMIT_NS, SHORT_NS)
     index = _expect_timeout(native, ctx, ctx.options(1e-8, 10000, "bsr", "jacobi", "mixed"))
     assert index >= 0  # the CTA whose wait ran out
