@@ -109,6 +109,7 @@ struct CgArgs {
         const void* inv;           // reciprocal pivots in schedule order
         int levels;
     } sw[2];
+    int staged_stash;              // mx_update_staged: nodes per CTA whose (z, p) stay in shared memory
     int sw_window;                 // ring slots per CTA (a power of two)
     int sw_maxp, sw_maxe;          // the largest piece: positions, entries (the stage size)
     void* sw_y;                    // forward result in backward positions (double or float)
@@ -433,13 +434,20 @@ __device__ __forceinline__ double2 precond64(const CgArgs& a, int i, double2 rv)
     return block2_apply(a.blk64, i, rv.x, rv.y);
 }
 
+// z of node i from the preconditioner's values pc (Jacobi: the inverse diagonal,
+// two floats a node; 2x2 blocks: the factor, three floats a node), wherever they are.
 template <int PRECOND>
-__device__ __forceinline__ float2 precond32(const CgArgs& a, int i, float2 rv) {
+__device__ __forceinline__ float2 precond32_at(const float* pc, int i, float2 rv) {
     if (PRECOND == LFGPU_PRECOND_JACOBI) {
-        const float2 d = reinterpret_cast<const float2*>(a.invd32)[i];
+        const float2 d = reinterpret_cast<const float2*>(pc)[i];
         return make_float2(d.x * rv.x, d.y * rv.y);
     }
-    return block2_apply32(a.blk32, i, rv.x, rv.y);
+    return block2_apply32(pc, i, rv.x, rv.y);
+}
+
+template <int PRECOND>
+__device__ __forceinline__ float2 precond32(const CgArgs& a, int i, float2 rv) {
+    return precond32_at<PRECOND>(PRECOND == LFGPU_PRECOND_JACOBI ? a.invd32 : a.blk32, i, rv);
 }
 
 #define GRID_NODES(i) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nb; i += gridDim.x * blockDim.x)
@@ -617,20 +625,20 @@ constexpr bool applied_separately() {
 }
 
 // DIRECT form, with the pointwise preconditioners (Jacobi, 2x2 nodal blocks) on
-// meshes of kDirectMinNodes nodes or more: mx_update also forms the next
-// direction.  Its CTAs, all resident (a cooperative launch), wait for the last one
-// to set beta and then rewrite p = z + beta p for their own nodes.  The product
-// then gathers p alone, 8 bytes a node instead of the (z, p_old) pair's 16, and
-// writes no p.  The values are those of forming p inside the product (the same
-// fma, once per node instead of once per gather), so the iterates do not change.
-// The wait costs a few microseconds whatever the size, the saving grows with it.
-// Per iteration of the mixed BSR/Jacobi solve on GB300 (n x n plane-strain
+// meshes of kDirectMinNodes nodes or more: the update (mx_update_staged) also
+// forms the next direction.  Its CTAs, all resident (a cooperative launch), wait
+// for the last one to set beta and then rewrite p = z + beta p for their own
+// nodes.  The product then gathers p alone, 8 bytes a node instead of the
+// (z, p_old) pair's 16, and writes no p.  p is the same fma of the same values as
+// when the product forms it, once per node instead of once per gather.  The wait
+// costs a few microseconds whatever the size, the saving grows with it.  Per
+// iteration of the mixed BSR/Jacobi solve on GB300 (n x n plane-strain
 // cantilevers, RCM), direct against (z, p_old) form: 400x400 (160,801 nodes)
-// 29.9 against 27.6 us; 600x600 (361,201) 39.6 against 36.1; 700x700 (491,401)
-// 43.3 against 42.2; 800x800 (641,601) 50.0 against 51.0; 1000x1000 (1,002,001)
-// 63.6 against 73.7.  The separately applied preconditioners keep the (z, p_old)
-// form: their z arrives after mx_update.
-constexpr long long kDirectMinNodes = 576000;
+// 27.05 against 26.93 us; 500x500 (251,001) 31.17 against 30.98; 600x600
+// (361,201) 35.77 against 36.02; 700x700 (491,401) 41.90 against 42.11; 800x800
+// (641,601) 47.69 against 50.66.  The separately applied preconditioners keep
+// the (z, p_old) form: their z arrives after mx_update.
+constexpr long long kDirectMinNodes = 300000;
 
 bool direct_form(int precond, long long nodes) {
     return (precond == LFGPU_PRECOND_JACOBI || precond == LFGPU_PRECOND_BLOCK2) && nodes >= kDirectMinNodes;
@@ -763,26 +771,72 @@ __device__ __forceinline__ unsigned ld_acquire_gpu_u32(const unsigned* p) {
     return v;
 }
 
-// x += alpha p (into the FP32 pair), r -= alpha q, z = M^-1 r; r.r and r.z; with
-// the direct form then p = z + beta p.
-template <int PRECOND, bool DIRECT>
-__global__ void __launch_bounds__(kThreads, 8) mx_update(CgArgs a) {  // 8 CTAs an SM: all 1,216 resident
-    constexpr bool kSub = applied_separately<PRECOND>();
-    constexpr bool kDirect = DIRECT;
-    static_assert(!(DIRECT && kSub), "the direct form needs a pointwise preconditioner");
-    // Jacobi: the second pass takes (z, p) of this thread's first kStash nodes from
-    // here (four cover 1,002,001 nodes on 1,216 CTAs of 256 threads) and reads r, p
-    // and the inverse diagonal of any further ones again.  The 2x2 blocks read all
-    // again: their update does not fit 32 registers with the stash.
-    constexpr int kStash = (kDirect && PRECOND == LFGPU_PRECOND_JACOBI) ? 4 : 0;
-    __shared__ float4 s_zp[kStash > 0 ? kStash : 1][kThreads];
+// The last CTA's step of the mixed update: iteration count, inner residual, the
+// replacement test, and (unless the preconditioner is applied separately) beta.
+template <bool SUB>
+__device__ __forceinline__ void update_totals(const CgArgs& a, const double* t) {
+    CgState* s = a.st;
+    s->it += 1;
+    const double rn = sqrt(fmax(0.0, t[0]));
+    s->rnorm = rn;
+    s->rmax = fmax(s->rmax, rn);
+    const bool refine = rn <= a.reduction * s->rmax || rn <= a.target || s->it >= a.maxit;
+    s->refine = refine;
+    if (!refine && !SUB) {
+        if (!(t[1] > 0.0) || !isfinite(t[1])) {
+            s->status = LFGPU_ERR_RHO;
+            s->done = 1;
+        } else {
+            s->beta = t[1] / s->rho;
+            s->beta32 = static_cast<float>(s->beta);
+            s->rho = t[1];
+        }
+    }
+    set_branch(a, refine && !s->done);
+    set_loop(a, !s->done);
+}
+
+// The direct form's grid-wide wait for beta (bounded), after update_totals ran in
+// the last CTA: true when the CTA goes on to form the direction.  A CTA whose wait
+// runs out ends the solve.  go0: CgState::go as the CTA found it at its start.
+__device__ __forceinline__ bool wait_for_beta(const CgArgs& a, bool last, unsigned go0) {
     __shared__ int s_go;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        if (last) {
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&a.st->go) : "memory");
+        } else {
+            // The wait lasts about one pass of the update; each poll is an L2
+            // round trip, so the limit is checked on every one.
+            const unsigned long long t0 = global_ns();
+            while (ld_acquire_gpu_u32(&a.st->go) == go0) {
+                if (wait_expired(a.status, t0, static_cast<int>(blockIdx.x))) {
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        if (!ok) {
+            a.st->done = 1;
+            set_branch(a, false);
+            set_loop(a, false);
+        }
+        s_go = ok && !__ldcg(&a.st->done) && !__ldcg(&a.st->refine);
+    }
+    __syncthreads();
+    return s_go != 0;
+}
+
+// x += alpha p (into the FP32 pair), r -= alpha q, z = M^-1 r; r.r and r.z.  The
+// (z, p_old) form: z goes into the pair copy the next product reads (the direct
+// form's update is mx_update_staged).
+template <int PRECOND>
+__global__ void __launch_bounds__(kThreads) mx_update(CgArgs a) {
+    constexpr bool kSub = applied_separately<PRECOND>();
     if (a.st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_branch(a, false);
         return;
     }
-    // The flag's value before any CTA arrives: it moves only after all have.
-    const unsigned go0 = kDirect ? a.st->go : 0u;
     const float alpha = a.st->alpha32, alpha_lo = a.st->alpha32_lo;
     const float2* p2 = reinterpret_cast<const float2*>(a.p32);
     const float2* q2 = reinterpret_cast<const float2*>(a.q32);
@@ -791,7 +845,6 @@ __global__ void __launch_bounds__(kThreads, 8) mx_update(CgArgs a) {  // 8 CTAs 
     float2* lo2 = reinterpret_cast<float2*>(a.xlo);
     float4* zp_next = zp_buffer(a, a.st->it + 1);
     FloatPair rr, rz;
-    int k = 0;
     GRID_NODES(i) {
         const float2 pv = p2[i], qv = q2[i];
         float2 hv = hi2[i], lv = lo2[i];
@@ -805,80 +858,12 @@ __global__ void __launch_bounds__(kThreads, 8) mx_update(CgArgs a) {  // 8 CTAs 
         hi2[i] = hv;
         lo2[i] = lv;
         r2[i] = rv;
-        if constexpr (kDirect) {
-            if (k < kStash) s_zp[k][threadIdx.x] = make_float4(zv.x, zv.y, pv.x, pv.y);
-            ++k;
-        } else {
-            zp_next[i] = make_float4(zv.x, pv.x, zv.y, pv.y);
-        }
+        zp_next[i] = make_float4(zv.x, pv.x, zv.y, pv.y);
         rr.add(rv.x * rv.x + rv.y * rv.y);
         if constexpr (!kSub) rz.add(rv.x * zv.x + rv.y * zv.y);
     }
     FloatPair v[2] = {rr, rz};
-    const bool last = reduce_last<2>(a, 2, v, [&](const double* t) {
-        CgState* s = a.st;
-        s->it += 1;
-        const double rn = sqrt(fmax(0.0, t[0]));
-        s->rnorm = rn;
-        s->rmax = fmax(s->rmax, rn);
-        const bool refine = rn <= a.reduction * s->rmax || rn <= a.target || s->it >= a.maxit;
-        s->refine = refine;
-        if (!refine && !kSub) {
-            if (!(t[1] > 0.0) || !isfinite(t[1])) {
-                s->status = LFGPU_ERR_RHO;
-                s->done = 1;
-            } else {
-                s->beta = t[1] / s->rho;
-                s->beta32 = static_cast<float>(s->beta);
-                s->rho = t[1];
-            }
-        }
-        set_branch(a, refine && !s->done);
-        set_loop(a, !s->done);
-    });
-    if constexpr (kDirect) {
-        // Grid-wide wait for beta (bounded).  A CTA whose wait runs out ends the solve.
-        if (threadIdx.x == 0) {
-            int ok = 1;
-            if (last) {
-                asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&a.st->go) : "memory");
-            } else {
-                // The wait lasts about one pass of the update; each poll is an L2
-                // round trip, so the limit is checked on every one.
-                const unsigned long long t0 = global_ns();
-                while (ld_acquire_gpu_u32(&a.st->go) == go0) {
-                    if (wait_expired(a.status, t0, static_cast<int>(blockIdx.x))) {
-                        ok = 0;
-                        break;
-                    }
-                }
-            }
-            if (!ok) {
-                a.st->done = 1;
-                set_branch(a, false);
-                set_loop(a, false);
-            }
-            s_go = ok && !__ldcg(&a.st->done) && !__ldcg(&a.st->refine);
-        }
-        __syncthreads();
-        if (!s_go) return;
-        const float beta = __ldcg(&a.st->beta32);
-        float2* pw = reinterpret_cast<float2*>(a.p32);
-        k = 0;
-        GRID_NODES(i) {  // this thread's nodes of the pass above
-            float2 zv, pv;
-            if (k < kStash) {
-                const float4 t = s_zp[k][threadIdx.x];
-                zv = make_float2(t.x, t.y);
-                pv = make_float2(t.z, t.w);
-            } else {
-                zv = precond32<PRECOND>(a, i, r2[i]);
-                pv = pw[i];
-            }
-            ++k;
-            pw[i] = make_float2(pnew(zv.x, pv.x, beta), pnew(zv.y, pv.y, beta));
-        }
-    }
+    reduce_last<2>(a, 2, v, [&](const double* t) { update_totals<kSub>(a, t); });
 }
 
 // After a residual replacement with a pointwise preconditioner: p = z + beta p, with
@@ -1673,6 +1658,139 @@ __global__ void __launch_bounds__(kThreads) precond_apply_kernel(CgArgs a) {
     GRID_NODES(i) { z2[i] = precond64<PRECOND>(a, i, r2[i]); }
 }
 
+// ------------------------------------------------------------------ staged mixed update
+// The direct form's update with its operands staged by TMA.  mx_update's threads
+// walk three or four nodes each, one round trip to memory per node, and the kernel
+// spends most of its time waiting on them (ncu: long-scoreboard and barrier
+// stalls, DRAM ~23 % busy).  Here each CTA owns a contiguous range of nodes, and
+// thread 0 copies it chunk by chunk (p, q, the correction pair, r and the
+// preconditioner's values of kStagedChunk nodes) into kStagedStages shared-memory
+// stages with cp.async.bulk, up to kStagedStages chunks ahead: ~50 KB in flight per
+// CTA instead of one load per thread.  The arithmetic per node is mx_update's, in
+// the same order.  (z, p) of the CTA's first staged_stash nodes stay in shared
+// memory for the direction pass; any further ones read r, p and the
+// preconditioner again from L2.
+constexpr int kStagedThreads = 256;  // one node per thread and chunk
+constexpr int kStagedChunk = kStagedThreads;
+constexpr int kStagedStages = 4;
+
+template <int PRECOND>
+constexpr int staged_pc_bytes() {  // preconditioner bytes per node
+    return PRECOND == LFGPU_PRECOND_JACOBI ? 8 : 12;
+}
+template <int PRECOND>
+constexpr int staged_stage_bytes() {  // p, q, hi, lo, r (8 bytes a node each) and the preconditioner
+    return kStagedChunk * (5 * 8 + staged_pc_bytes<PRECOND>());
+}
+// Nodes of CTA b: [b * per, min(nb, (b + 1) * per)) with per a multiple of 4, so that
+// every copy starts on a 16-byte boundary.  A copy's node count is rounded up to 4:
+// the vectors' allocations are padded to 64 elements, the 2x2 factor by 12 floats.
+inline __host__ __device__ int staged_per_cta(int nb, int grid) { return ((nb + grid - 1) / grid + 3) & ~3; }
+
+template <int PRECOND>
+__global__ void __launch_bounds__(kStagedThreads) mx_update_staged(CgArgs a) {
+    constexpr int C = kStagedChunk, S = kStagedStages, PCB = staged_pc_bytes<PRECOND>();
+    constexpr int SB = staged_stage_bytes<PRECOND>();
+    extern __shared__ __align__(128) unsigned char staged_smem[];
+    __shared__ __align__(8) unsigned long long full[S];
+    __shared__ int s_failed;
+    if (a.st->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) set_branch(a, false);
+        return;
+    }
+    const unsigned go0 = a.st->go;  // moves only after every CTA has arrived
+    const float alpha = a.st->alpha32, alpha_lo = a.st->alpha32_lo;
+    const int tid = threadIdx.x;
+    const int per = staged_per_cta(a.nb, gridDim.x);
+    const int n0 = min(a.nb, static_cast<int>(blockIdx.x) * per), n1 = min(a.nb, n0 + per);
+    const int chunks = (n1 - n0 + C - 1) / C;
+    const int stash_n = min(n1 - n0, a.staged_stash);
+    float4* stash = reinterpret_cast<float4*>(staged_smem + S * SB);  // (z, p) of node n0 + j, j < stash_n
+    const float* pc = PRECOND == LFGPU_PRECOND_JACOBI ? a.invd32 : a.blk32;
+    auto issue = [&](int k) {  // thread 0: chunk k into stage k % S
+        const int s = k % S, b = n0 + k * C;
+        const unsigned cnt4 = static_cast<unsigned>((min(C, n1 - b) + 3) & ~3);
+        unsigned char* st = staged_smem + s * SB;
+        mbar_expect_tx(full + s, cnt4 * (5u * 8u + static_cast<unsigned>(PCB)));
+        bulk_copy(st, a.p32 + 2 * static_cast<size_t>(b), cnt4 * 8u, full + s);
+        bulk_copy(st + C * 8, a.q32 + 2 * static_cast<size_t>(b), cnt4 * 8u, full + s);
+        bulk_copy(st + 2 * C * 8, a.xhi + 2 * static_cast<size_t>(b), cnt4 * 8u, full + s);
+        bulk_copy(st + 3 * C * 8, a.xlo + 2 * static_cast<size_t>(b), cnt4 * 8u, full + s);
+        bulk_copy(st + 4 * C * 8, a.r32 + 2 * static_cast<size_t>(b), cnt4 * 8u, full + s);
+        bulk_copy(st + 5 * C * 8, pc + (PCB / 4) * static_cast<size_t>(b), cnt4 * static_cast<unsigned>(PCB), full + s);
+    };
+    if (tid == 0) {
+        s_failed = 0;
+        for (int s = 0; s < S; ++s) mbar_init(full + s, 1);
+        mbar_init_fence();
+        for (int k = 0; k < S && k < chunks; ++k) issue(k);
+    }
+    __syncthreads();
+    const unsigned long long limit = a.status->wait_limit_ns;
+    bool ok = true;
+    FloatPair rr, rz;
+    for (int k = 0; k < chunks; ++k) {
+        const int s = k % S;
+        ok = mbar_wait(full + s, static_cast<unsigned>(k / S) & 1u, a.status, limit) && ok;
+        const unsigned char* st = staged_smem + s * SB;
+        const int i = n0 + k * C + tid;
+        if (i < n1) {
+            const float2 pv = reinterpret_cast<const float2*>(st)[tid];
+            const float2 qv = reinterpret_cast<const float2*>(st + C * 8)[tid];
+            float2 hv = reinterpret_cast<const float2*>(st + 2 * C * 8)[tid];
+            float2 lv = reinterpret_cast<const float2*>(st + 3 * C * 8)[tid];
+            float2 rv = reinterpret_cast<const float2*>(st + 4 * C * 8)[tid];
+            pair_axpy(hv.x, lv.x, alpha, alpha_lo, pv.x);
+            pair_axpy(hv.y, lv.y, alpha, alpha_lo, pv.y);
+            rv.x -= alpha * qv.x;
+            rv.y -= alpha * qv.y;
+            const float2 zv = precond32_at<PRECOND>(reinterpret_cast<const float*>(st + 5 * C * 8), tid, rv);
+            reinterpret_cast<float2*>(a.xhi)[i] = hv;
+            reinterpret_cast<float2*>(a.xlo)[i] = lv;
+            reinterpret_cast<float2*>(a.r32)[i] = rv;
+            if (i - n0 < stash_n) stash[i - n0] = make_float4(zv.x, zv.y, pv.x, pv.y);
+            rr.add(rv.x * rv.x + rv.y * rv.y);
+            rz.add(rv.x * zv.x + rv.y * zv.y);
+        }
+        __syncthreads();  // every thread is done with stage s
+        if (tid == 0 && k + S < chunks) issue(k + S);
+    }
+    if (!ok) s_failed = 1;
+    __syncthreads();
+    if (s_failed) {
+        // A copy did not arrive in time: end the solve (the status word says why),
+        // and give copies still on their way into this CTA's stages time to land
+        // before its shared memory is released.
+        if (tid == 0) {
+            a.st->done = 1;
+            set_branch(a, false);
+            set_loop(a, false);
+            const unsigned long long t0 = global_ns();
+            while (global_ns() - t0 < 100000ull) {
+            }
+        }
+        __syncthreads();
+        return;
+    }
+    FloatPair v[2] = {rr, rz};
+    const bool last = reduce_last<2>(a, 2, v, [&](const double* t) { update_totals<false>(a, t); });
+    if (!wait_for_beta(a, last, go0)) return;
+    const float beta = __ldcg(&a.st->beta32);
+    float2* pw = reinterpret_cast<float2*>(a.p32);
+    for (int j = n0 + tid; j < n1; j += C) {  // the nodes this thread updated above
+        float2 zv, pv;
+        if (j - n0 < stash_n) {
+            const float4 t = stash[j - n0];
+            zv = make_float2(t.x, t.y);
+            pv = make_float2(t.z, t.w);
+        } else {
+            zv = precond32<PRECOND>(a, j, reinterpret_cast<const float2*>(a.r32)[j]);
+            pv = pw[j];
+        }
+        pw[j] = make_float2(pnew(zv.x, pv.x, beta), pnew(zv.y, pv.y, beta));
+    }
+}
+
 // ------------------------------------------------------------------ graph assembly
 struct GraphBuilder {
     Context& c;
@@ -1700,15 +1818,27 @@ void add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep
     }
 }
 
-// CTAs of a kernel that waits on a grid-wide flag: at most `want`, and no more than
-// the device keeps resident at once.
-template <typename K>
-int resident_grid(K kernel, int want) {
-    int dev = 0, sms = 0, per_sm = 0;
+// Launch shape of mx_update_staged: two CTAs an SM (fewer if they do not fit), the
+// stages, and the rest of each CTA's half of the SM's shared memory for (z, p).
+struct StagedShape {
+    int grid, smem, stash;
+};
+template <int PRECOND>
+StagedShape staged_shape(int nb) {
+    int dev = 0, sms = 0, smem_sm = 0, per_sm = 0;
     LF_CUDA(cudaGetDevice(&dev));
     LF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    LF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0));
-    return std::max(1, std::min(want, per_sm * sms));
+    LF_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    const int stages = kStagedStages * staged_stage_bytes<PRECOND>();
+    const int half = smem_sm / 2 - 4096;  // less the static arrays and the per-CTA reservation
+    const int grid = 2 * sms;
+    const int stash = std::max(0, std::min((half - stages) / 16, staged_per_cta(nb, grid)));
+    StagedShape sh{grid, stages + 16 * stash, stash};
+    LF_CUDA(cudaFuncSetAttribute(mx_update_staged<PRECOND>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem));
+    LF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx_update_staged<PRECOND>, kStagedThreads, sh.smem));
+    LF_REQUIRE(per_sm >= 1, LFGPU_ERR_CUDA, "the staged update does not fit an SM");
+    sh.grid = std::min(grid, per_sm * sms);
+    return sh;
 }
 
 cudaGraphNode_t add_conditional(cudaGraph_t g, const cudaGraphNode_t* dep, int ndep, cudaGraphConditionalHandle h,
@@ -1766,7 +1896,11 @@ template <int STORAGE, int PRECOND, bool DIRECT>
 void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub_threads = 0, int smem = 0) {
     constexpr bool kSub = applied_separately<PRECOND>();
     constexpr bool kDirect = DIRECT;
-    const int update_grid = kDirect ? resident_grid(mx_update<PRECOND, DIRECT>, blocks) : blocks;
+    StagedShape sh{blocks, 0, 0};
+    if constexpr (kDirect) {
+        sh = staged_shape<PRECOND>(a->nb);
+        a->staged_stash = sh.stash;
+    }
     cudaGraphNode_t n_init;
     add_kernel(g, &n_init, nullptr, 0, mx_init<PRECOND, DIRECT>, blocks, a);
     if constexpr (kSub) n_init = add_mixed_apply<PRECOND>(g, n_init, a, sub_grid, sub_threads, smem);
@@ -1786,7 +1920,10 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub
         LF_CUDA(cudaGraphConditionalHandleCreate(&ah->branch, body, 0, 0));
         cudaGraphNode_t k1, k2, k3, k4, k5, k6;
         add_kernel(body, &k1, prev ? &prev : nullptr, prev ? 1 : 0, mx_product<STORAGE, kDirect>, blocks, ah);
-        add_kernel(body, &k2, &k1, 1, mx_update<PRECOND, DIRECT>, update_grid, ah, 0, kThreads, kDirect);
+        if constexpr (kDirect)
+            add_kernel(body, &k2, &k1, 1, mx_update_staged<PRECOND>, sh.grid, ah, sh.smem, kStagedThreads, true);
+        else
+            add_kernel(body, &k2, &k1, 1, mx_update<PRECOND>, blocks, ah);
         cudaGraph_t branch;
         prev = add_conditional(body, &k2, 1, ah->branch, cudaGraphCondTypeIf, &branch);
         add_kernel(branch, &k3, nullptr, 0, mx_flush<false>, blocks, ah);
@@ -1860,15 +1997,19 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
         trail.mark(phase);
     };
     constexpr bool kDirect = DIRECT;
+    StagedShape sh{blocks, 0, 0};
+    if constexpr (kDirect) {
+        sh = staged_shape<PRECOND>(a->nb);
+        a->staged_stash = sh.stash;
+    }
     auto update = [&](int phase) {
         if constexpr (kDirect) {  // its CTAs wait for one another: a cooperative launch
             void* args[1] = {a};
-            LF_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(mx_update<PRECOND, DIRECT>),
-                                                dim3(resident_grid(mx_update<PRECOND, DIRECT>, blocks)),
-                                                dim3(kThreads), args, 0, stream));
+            LF_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(mx_update_staged<PRECOND>), dim3(sh.grid),
+                                                dim3(kStagedThreads), args, static_cast<size_t>(sh.smem), stream));
             trail.mark(phase);
         } else {
-            chain(mx_update<PRECOND, DIRECT>, phase);
+            chain(mx_update<PRECOND>, phase);
         }
     };
     if (!mixed && a->x0) chain(cg64_residual<STORAGE>, -1);

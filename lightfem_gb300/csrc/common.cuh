@@ -453,6 +453,14 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned b
         : "memory");
 }
 
+// The same without an L2 policy (data the next kernels read again).
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
 // Order this CTA's earlier generic-proxy shared-memory accesses before later bulk copies.
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 

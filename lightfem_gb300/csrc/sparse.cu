@@ -609,7 +609,7 @@ static void setup_preconditioners(Context& c) {
     c.inv_diag64.ensure(c.n);
     c.blk64.ensure(3 * static_cast<size_t>(nb));
     c.inv_diag32.ensure(c.n);
-    c.blk32.ensure(3 * static_cast<size_t>(nb));
+    c.blk32.ensure(3 * static_cast<size_t>(nb) + 12);  // the staged update copies whole groups of four nodes
     c.scratch64.ensure(64);
     // flags[0]: degenerate 2x2 blocks; flags[1]: first non-finite diagonal DOF.
     int* flags = reinterpret_cast<int*>(c.scratch64.p + 8);
