@@ -1673,6 +1673,7 @@ __global__ void __launch_bounds__(kThreads) precond_apply_kernel(CgArgs a) {
 constexpr int kStagedThreads = 256;  // one node per thread and chunk
 constexpr int kStagedChunk = kStagedThreads;
 constexpr int kStagedStages = 4;
+constexpr int kStagedCtasPerSm = 2;
 
 template <int PRECOND>
 constexpr int staged_pc_bytes() {  // preconditioner bytes per node
@@ -1818,8 +1819,9 @@ void add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* dep
     }
 }
 
-// Launch shape of mx_update_staged: two CTAs an SM (fewer if they do not fit), the
-// stages, and the rest of each CTA's half of the SM's shared memory for (z, p).
+// Launch shape of mx_update_staged: kStagedCtasPerSm CTAs an SM (fewer if they do
+// not fit), the stages, and the rest of each CTA's share of the SM's shared memory
+// for (z, p).
 struct StagedShape {
     int grid, smem, stash;
 };
@@ -1830,9 +1832,9 @@ StagedShape staged_shape(int nb) {
     LF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     LF_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     const int stages = kStagedStages * staged_stage_bytes<PRECOND>();
-    const int half = smem_sm / 2 - 4096;  // less the static arrays and the per-CTA reservation
-    const int grid = 2 * sms;
-    const int stash = std::max(0, std::min((half - stages) / 16, staged_per_cta(nb, grid)));
+    const int share = smem_sm / kStagedCtasPerSm - 4096;  // less the static arrays and the per-CTA reservation
+    const int grid = kStagedCtasPerSm * sms;
+    const int stash = std::max(0, std::min((share - stages) / 16, staged_per_cta(nb, grid)));
     StagedShape sh{grid, stages + 16 * stash, stash};
     LF_CUDA(cudaFuncSetAttribute(mx_update_staged<PRECOND>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem));
     LF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx_update_staged<PRECOND>, kStagedThreads, sh.smem));
