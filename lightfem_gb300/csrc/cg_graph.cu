@@ -1663,15 +1663,20 @@ __global__ void __launch_bounds__(kThreads) precond_apply_kernel(CgArgs a) {
 // walk three or four nodes each, one round trip to memory per node, and the kernel
 // spends most of its time waiting on them (ncu: long-scoreboard and barrier
 // stalls, DRAM ~23 % busy).  Here each CTA owns a contiguous range of nodes, and
-// thread 0 copies it chunk by chunk (p, q, the correction pair, r and the
+// a producer warp copies it chunk by chunk (p, q, the correction pair, r and the
 // preconditioner's values of kStagedChunk nodes) into kStagedStages shared-memory
 // stages with cp.async.bulk, up to kStagedStages chunks ahead: ~50 KB in flight per
-// CTA instead of one load per thread.  The arithmetic per node is mx_update's, in
-// the same order.  (z, p) of the CTA's first staged_stash nodes stay in shared
-// memory for the direction pass; any further ones read r, p and the
-// preconditioner again from L2.
-constexpr int kStagedThreads = 256;  // one node per thread and chunk
+// CTA instead of one load per thread.  It refills a stage as soon as every
+// consumer warp has arrived on the stage's empty barrier, so no block-wide barrier
+// runs per chunk (the 1000x1000 mixed BSR/Jacobi solve on one GB300: 1,032 ms with
+// thread 0 refilling after a __syncthreads, 1,016 ms with the producer warp, 1,025
+// ms with six stages).  The arithmetic per node is mx_update's, in the same order.
+// (z, p) of the CTA's first staged_stash nodes stay in shared memory for the
+// direction pass; any further ones read r, p and the preconditioner again from L2.
+constexpr int kStagedThreads = 256;  // consumers: one node per thread and chunk
 constexpr int kStagedChunk = kStagedThreads;
+constexpr int kStagedBlock = kStagedThreads + 32;  // plus the producer warp
+constexpr int kStagedWarps = kStagedThreads / 32;
 constexpr int kStagedStages = 4;
 constexpr int kStagedCtasPerSm = 2;
 
@@ -1689,11 +1694,11 @@ constexpr int staged_stage_bytes() {  // p, q, hi, lo, r (8 bytes a node each) a
 inline __host__ __device__ int staged_per_cta(int nb, int grid) { return ((nb + grid - 1) / grid + 3) & ~3; }
 
 template <int PRECOND>
-__global__ void __launch_bounds__(kStagedThreads) mx_update_staged(CgArgs a) {
+__global__ void __launch_bounds__(kStagedBlock) mx_update_staged(CgArgs a) {
     constexpr int C = kStagedChunk, S = kStagedStages, PCB = staged_pc_bytes<PRECOND>();
     constexpr int SB = staged_stage_bytes<PRECOND>();
     extern __shared__ __align__(128) unsigned char staged_smem[];
-    __shared__ __align__(8) unsigned long long full[S];
+    __shared__ __align__(8) unsigned long long full[S], empty[S];
     __shared__ int s_failed;
     if (a.st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_branch(a, false);
@@ -1708,7 +1713,7 @@ __global__ void __launch_bounds__(kStagedThreads) mx_update_staged(CgArgs a) {
     const int stash_n = min(n1 - n0, a.staged_stash);
     float4* stash = reinterpret_cast<float4*>(staged_smem + S * SB);  // (z, p) of node n0 + j, j < stash_n
     const float* pc = PRECOND == LFGPU_PRECOND_JACOBI ? a.invd32 : a.blk32;
-    auto issue = [&](int k) {  // thread 0: chunk k into stage k % S
+    auto issue = [&](int k) {  // the producer: chunk k into stage k % S
         const int s = k % S, b = n0 + k * C;
         const unsigned cnt4 = static_cast<unsigned>((min(C, n1 - b) + 3) & ~3);
         unsigned char* st = staged_smem + s * SB;
@@ -1722,14 +1727,26 @@ __global__ void __launch_bounds__(kStagedThreads) mx_update_staged(CgArgs a) {
     };
     if (tid == 0) {
         s_failed = 0;
-        for (int s = 0; s < S; ++s) mbar_init(full + s, 1);
+        for (int s = 0; s < S; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, kStagedWarps);
+        }
         mbar_init_fence();
-        for (int k = 0; k < S && k < chunks; ++k) issue(k);
     }
     __syncthreads();
     const unsigned long long limit = a.status->wait_limit_ns;
     bool ok = true;
     FloatPair rr, rz;
+    if (tid >= kStagedThreads) {
+        // Producer warp: lane 0 refills a stage as soon as every consumer warp is done with it.
+        if (tid == kStagedThreads) {
+            for (int k = 0; k < chunks; ++k) {
+                const int s = k % S;
+                if (k >= S) ok = mbar_wait(empty + s, static_cast<unsigned>(k / S - 1) & 1u, a.status, limit) && ok;
+                issue(k);
+            }
+        }
+    } else {
     for (int k = 0; k < chunks; ++k) {
         const int s = k % S;
         ok = mbar_wait(full + s, static_cast<unsigned>(k / S) & 1u, a.status, limit) && ok;
@@ -1753,8 +1770,9 @@ __global__ void __launch_bounds__(kStagedThreads) mx_update_staged(CgArgs a) {
             rr.add(rv.x * rv.x + rv.y * rv.y);
             rz.add(rv.x * zv.x + rv.y * zv.y);
         }
-        __syncthreads();  // every thread is done with stage s
-        if (tid == 0 && k + S < chunks) issue(k + S);
+        __syncwarp();
+        if ((tid & 31) == 0) arrive(empty + s);  // this warp is done with stage s
+    }
     }
     if (!ok) s_failed = 1;
     __syncthreads();
@@ -1778,7 +1796,7 @@ __global__ void __launch_bounds__(kStagedThreads) mx_update_staged(CgArgs a) {
     if (!wait_for_beta(a, last, go0)) return;
     const float beta = __ldcg(&a.st->beta32);
     float2* pw = reinterpret_cast<float2*>(a.p32);
-    for (int j = n0 + tid; j < n1; j += C) {  // the nodes this thread updated above
+    for (int j = n0 + tid; tid < C && j < n1; j += C) {  // the nodes this thread updated above
         float2 zv, pv;
         if (j - n0 < stash_n) {
             const float4 t = stash[j - n0];
@@ -1837,7 +1855,7 @@ StagedShape staged_shape(int nb) {
     const int stash = std::max(0, std::min((share - stages) / 16, staged_per_cta(nb, grid)));
     StagedShape sh{grid, stages + 16 * stash, stash};
     LF_CUDA(cudaFuncSetAttribute(mx_update_staged<PRECOND>, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem));
-    LF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx_update_staged<PRECOND>, kStagedThreads, sh.smem));
+    LF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mx_update_staged<PRECOND>, kStagedBlock, sh.smem));
     LF_REQUIRE(per_sm >= 1, LFGPU_ERR_CUDA, "the staged update does not fit an SM");
     sh.grid = std::min(grid, per_sm * sms);
     return sh;
@@ -1923,7 +1941,7 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub
         cudaGraphNode_t k1, k2, k3, k4, k5, k6;
         add_kernel(body, &k1, prev ? &prev : nullptr, prev ? 1 : 0, mx_product<STORAGE, kDirect>, blocks, ah);
         if constexpr (kDirect)
-            add_kernel(body, &k2, &k1, 1, mx_update_staged<PRECOND>, sh.grid, ah, sh.smem, kStagedThreads, true);
+            add_kernel(body, &k2, &k1, 1, mx_update_staged<PRECOND>, sh.grid, ah, sh.smem, kStagedBlock, true);
         else
             add_kernel(body, &k2, &k1, 1, mx_update<PRECOND>, blocks, ah);
         cudaGraph_t branch;
@@ -2008,7 +2026,7 @@ void launch_unrolled(cudaStream_t stream, CgArgs* a, int blocks, bool mixed, int
         if constexpr (kDirect) {  // its CTAs wait for one another: a cooperative launch
             void* args[1] = {a};
             LF_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(mx_update_staged<PRECOND>), dim3(sh.grid),
-                                                dim3(kStagedThreads), args, static_cast<size_t>(sh.smem), stream));
+                                                dim3(kStagedBlock), args, static_cast<size_t>(sh.smem), stream));
             trail.mark(phase);
         } else {
             chain(mx_update<PRECOND>, phase);
