@@ -51,6 +51,11 @@ struct CgState {
     // it before they form the next direction (only equality with the value a CTA
     // saw at its start matters, so it may wrap).
     unsigned int go, pad_go;
+    // The values last written to the graph's conditional handles (the WHILE loop's
+    // and each body iteration's IF), so that a kernel writes one only when it
+    // changes: cudaGraphSetConditional costs a noticeable part of a microsecond.
+    // 0: not written yet in this solve, 1: false, 2: true.
+    int loop_val, branch_val[8];
 };
 
 struct CgArgs {
@@ -122,14 +127,25 @@ struct CgArgs {
     long long maxit, max_ref;
     int restart;
     int use_cond;  // 0 in the unrolled profiling graph, which has no conditional nodes
+    int half;      // the body iteration (0 .. 7) whose IF handle `branch` is
     cudaGraphConditionalHandle loop, branch;
 };
 
+// A handle keeps its value from one evaluation to the next.  Every solve starts
+// from a zeroed CgState, so the first call of each solve writes the handle.
 __device__ __forceinline__ void set_loop(const CgArgs& a, bool go) {
-    if (a.use_cond) cudaGraphSetConditional(a.loop, go ? 1u : 0u);
+    const int want = go ? 2 : 1;
+    if (a.use_cond && a.st->loop_val != want) {
+        cudaGraphSetConditional(a.loop, go ? 1u : 0u);
+        a.st->loop_val = want;
+    }
 }
 __device__ __forceinline__ void set_branch(const CgArgs& a, bool go) {
-    if (a.use_cond) cudaGraphSetConditional(a.branch, go ? 1u : 0u);
+    const int want = go ? 2 : 1;
+    if (a.use_cond && a.st->branch_val[a.half] != want) {
+        cudaGraphSetConditional(a.branch, go ? 1u : 0u);
+        a.st->branch_val[a.half] = want;
+    }
 }
 
 // Block sums of K values, then the last block to finish adds every block's sums in
@@ -191,11 +207,12 @@ struct FloatPair {
     }
 };
 
-// FP32-pair per-thread values (the mixed inner loop): warp sums as pairs, the
-// warps' sums added in FP64 by thread 0.
-template <int K, typename Final>
-__device__ __forceinline__ bool reduce_last(const CgArgs& a, int slot, FloatPair (&v)[K], Final&& fin) {
-    __shared__ double s_red[32 * kMaxReduce];
+// FP32-pair per-thread values summed over the CTA (the mixed inner loop): warp
+// sums as pairs, then the warps' pairs in warp 0, whose threads all get the CTA's
+// totals as pairs in w (the other threads' w is zero).  FP32 arithmetic only: on
+// GB300 a dependent FP64 add takes about as long as a dozen FP32 ones.
+template <int K>
+__device__ __forceinline__ void block_pair_reduce(FloatPair (&v)[K], FloatPair (&w)[K]) {
     __shared__ float2 s_warp[32 * kMaxReduce];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -213,30 +230,75 @@ __device__ __forceinline__ bool reduce_last(const CgArgs& a, int slot, FloatPair
         for (int k = 0; k < K; ++k) s_warp[warp * K + k] = make_float2(v[k].hi, v[k].lo);
     }
     __syncthreads();
-    double d[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) d[k] = 0.0;
+    for (int k = 0; k < K; ++k) w[k] = FloatPair{};
     if (warp == 0) {
         const int nw = blockDim.x >> 5;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            FloatPair w;
             if (lane < nw) {
                 const float2 t = s_warp[lane * K + k];
-                w.hi = t.x;
-                w.lo = t.y;
+                w[k].hi = t.x;
+                w[k].lo = t.y;
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 FloatPair other;
-                other.hi = __shfl_xor_sync(0xffffffffu, w.hi, o);
-                other.lo = __shfl_xor_sync(0xffffffffu, w.lo, o);
-                w.add(other);
+                other.hi = __shfl_xor_sync(0xffffffffu, w[k].hi, o);
+                other.lo = __shfl_xor_sync(0xffffffffu, w[k].lo, o);
+                w[k].add(other);
             }
-            d[k] = static_cast<double>(w.hi) + static_cast<double>(w.lo);
         }
     }
-    return reduce_tail<K>(a, slot, d, s_red, fin);
+    __syncthreads();  // s_warp is free again
+}
+
+// The grid-wide step for FP32-pair values: each CTA leaves its pair totals, and
+// the last CTA to arrive adds all CTAs' pairs, in a fixed assignment to its threads
+// and a fixed shuffle tree (deterministic), then runs fin on the FP64 values
+// hi + lo.  Pairs instead of FP64 partials keep the last CTA's tail, which the
+// rest of the iteration waits for, off GB300's slow FP64 adds.  Returns true in
+// the last CTA.
+template <int K, typename Final>
+__device__ __forceinline__ bool reduce_tail_pair(const CgArgs& a, int slot, const FloatPair (&w)[K], Final&& fin) {
+    __shared__ int s_last;
+    float2* part = reinterpret_cast<float2*>(a.partials + static_cast<size_t>(slot) * a.blocks * kMaxReduce);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) part[blockIdx.x * kMaxReduce + k] = make_float2(w[k].hi, w[k].lo);
+        unsigned t;  // arrive with release semantics: the partials above are visible first
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(t) : "l"(&a.st->count[slot]) : "memory");
+        s_last = t == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    FloatPair acc[K];
+    for (int b = threadIdx.x; b < static_cast<int>(gridDim.x); b += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const float2 t = __ldcg(part + b * kMaxReduce + k);
+            acc[k].add(FloatPair{t.x, t.y});
+        }
+    }
+    FloatPair tot[K];
+    block_pair_reduce<K>(acc, tot);
+    if (threadIdx.x == 0) {
+        double d[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) d[k] = static_cast<double>(tot[k].hi) + static_cast<double>(tot[k].lo);
+        a.st->count[slot] = 0;
+        fin(d);
+    }
+    return true;
+}
+
+// FP32-pair per-thread values: pair sums within the CTA, then across the grid.
+template <int K, typename Final>
+__device__ __forceinline__ bool reduce_last(const CgArgs& a, int slot, FloatPair (&v)[K], Final&& fin) {
+    FloatPair w[K];
+    block_pair_reduce<K>(v, w);
+    return reduce_tail_pair<K>(a, slot, w, fin);
 }
 
 // Warp-uniform loop over row groups of 8 (quarter warp per row) across the grid.
@@ -616,6 +678,23 @@ __device__ __forceinline__ void pair_axpy(float& hi, float& lo, float ah, float 
     lo = __fsub_rn(l, __fsub_rn(hi, s));
 }
 
+// num / den as an unevaluated FP32 pair (hi + lo, about 44 bits; Dekker's
+// division): one FP32 quotient, its remainder from an error-free product, and a
+// correction.  The loop's scalars (alpha, beta) come from this instead of an FP64
+// division, whose dependent steps take a large part of a microsecond on GB300
+// and hold up every CTA waiting for them.
+__device__ __forceinline__ void pair_quotient(double num, double den, float& hi, float& lo) {
+    const float nh = static_cast<float>(num), nl = static_cast<float>(num - static_cast<double>(nh));
+    const float dh = static_cast<float>(den), dl = static_cast<float>(den - static_cast<double>(dh));
+    const float q1 = __fdiv_rn(nh, dh);
+    const float p = __fmul_rn(q1, dh);
+    const float pe = __fmaf_rn(q1, dh, -p);  // q1 * dh = p + pe exactly
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(nh, p), pe), __fsub_rn(nl, __fmul_rn(q1, dl)));
+    const float q2 = __fdiv_rn(r, dh);
+    hi = __fadd_rn(q1, q2);
+    lo = __fsub_rn(q2, __fsub_rn(hi, q1));
+}
+
 // Preconditioners applied by their own kernels (the subdomain block solves,
 // mx_sub_apply; the IC(0) sweeps, ic0_level_sweep) run after mx_init and after
 // every mx_update: those two leave z and r.z to them.
@@ -758,9 +837,8 @@ __global__ void __launch_bounds__(kThreads) mx_product(CgArgs a) {
             s->done = 1;
             set_loop(a, false);
         } else {
-            s->alpha = s->rho / t[0];
-            s->alpha32 = static_cast<float>(s->alpha);
-            s->alpha32_lo = static_cast<float>(s->alpha - static_cast<double>(s->alpha32));
+            pair_quotient(s->rho, t[0], s->alpha32, s->alpha32_lo);
+            s->alpha = static_cast<double>(s->alpha32) + static_cast<double>(s->alpha32_lo);
         }
     });
 }
@@ -777,7 +855,9 @@ template <bool SUB>
 __device__ __forceinline__ void update_totals(const CgArgs& a, const double* t) {
     CgState* s = a.st;
     s->it += 1;
-    const double rn = sqrt(fmax(0.0, t[0]));
+    // The inner residual norm only decides when to replace the residual: FP32 is
+    // enough, and an FP64 square root would hold up the grid.
+    const double rn = static_cast<double>(__fsqrt_rn(static_cast<float>(fmax(0.0, t[0]))));
     s->rnorm = rn;
     s->rmax = fmax(s->rmax, rn);
     const bool refine = rn <= a.reduction * s->rmax || rn <= a.target || s->it >= a.maxit;
@@ -787,8 +867,9 @@ __device__ __forceinline__ void update_totals(const CgArgs& a, const double* t) 
             s->status = LFGPU_ERR_RHO;
             s->done = 1;
         } else {
-            s->beta = t[1] / s->rho;
-            s->beta32 = static_cast<float>(s->beta);
+            float lo;
+            pair_quotient(t[1], s->rho, s->beta32, lo);
+            s->beta = static_cast<double>(s->beta32) + static_cast<double>(lo);
             s->rho = t[1];
         }
     }
@@ -1183,9 +1264,14 @@ __device__ __forceinline__ void rho_from_application(const CgArgs& a, const doub
     if (!(t[0] > 0.0) || !isfinite(t[0])) {
         st->status = first ? LFGPU_ERR_RHO_INITIAL : LFGPU_ERR_RHO;
         st->done = 1;
+    } else if (first || (a.restart && st->refine)) {
+        st->beta = 0.0;
+        st->beta32 = 0.f;
+        st->rho = t[0];
     } else {
-        st->beta = (first || (a.restart && st->refine)) ? 0.0 : t[0] / st->rho;
-        st->beta32 = static_cast<float>(st->beta);
+        float lo;
+        pair_quotient(t[0], st->rho, st->beta32, lo);
+        st->beta = static_cast<double>(st->beta32) + static_cast<double>(lo);
         st->rho = t[0];
     }
     set_loop(a, !st->done);
@@ -1937,6 +2023,7 @@ void build_mixed(cudaGraph_t g, CgArgs* a, int blocks, int sub_grid = 0, int sub
     for (int h = 0; h < kBodyIterations; ++h) {
         halves[h] = *a;
         CgArgs* ah = &halves[h];
+        ah->half = h;
         LF_CUDA(cudaGraphConditionalHandleCreate(&ah->branch, body, 0, 0));
         cudaGraphNode_t k1, k2, k3, k4, k5, k6;
         add_kernel(body, &k1, prev ? &prev : nullptr, prev ? 1 : 0, mx_product<STORAGE, kDirect>, blocks, ah);
