@@ -45,11 +45,11 @@ struct CgState {
     unsigned int count[4];
     // FP32 copies for the mixed loop, set where alpha and beta are, so that no
     // thread of the loop kernels converts them (GB300's FP64 pipe is narrow):
-    // alpha = alpha32 + alpha32_lo to about 48 bits.
+    // alpha = alpha32 + alpha32_lo to about 44 bits (pair_quotient).
     float alpha32, alpha32_lo, beta32, pad32;
-    // Raised by the last CTA of mx_update once beta is set; the other CTAs wait for
-    // it before they form the next direction (only equality with the value a CTA
-    // saw at its start matters, so it may wrap).
+    // Raised by the last CTA of mx_update_staged once beta is set; the other CTAs
+    // wait for it before they form the next direction (only equality with the
+    // value a CTA saw at its start matters, so it may wrap).
     unsigned int go, pad_go;
     // The values last written to the graph's conditional handles (the WHILE loop's
     // and each body iteration's IF), so that a kernel writes one only when it
@@ -712,12 +712,13 @@ __global__ void __launch_bounds__(kThreads) cg64_direction(CgArgs a) {
 
 // ------------------------------------------------------------------ mixed kernels
 // FP32 vectors of the inner solve.  In the direct form (see kDirectMinNodes) p is
-// a plain vector that mx_update rewrites.  Otherwise z and p are interleaved per DOF, (z_c, p_c), so the product gathers
-// both with one 16-byte load per node and forms p; two copies alternate between
-// iterations (the product reads one, the update writes the other).  The solution correction since the last residual replacement is kept
-// as an unevaluated FP32 pair (hi + lo, about 48 significant bits) and added to
-// the FP64 solution when a replacement is due, so no FP64 arithmetic runs per
-// iteration.
+// a plain vector that mx_update_staged rewrites.  Otherwise z and p are
+// interleaved per DOF, (z_c, p_c), so the product gathers both with one 16-byte
+// load per node and forms p; two copies alternate between iterations (the product
+// reads one, the update writes the other).  The solution correction since the
+// last residual replacement is kept as an unevaluated FP32 pair (hi + lo, about
+// 48 significant bits) and added to the FP64 solution when a replacement is due,
+// so no FP64 arithmetic runs per iteration.
 __device__ __forceinline__ float pnew(float z, float p, float beta) { return __fmaf_rn(beta, p, z); }
 __device__ __forceinline__ float with_diag(float off, float hi, float lo, float x) { return fmaf(hi, x, off) + lo * x; }
 
@@ -828,7 +829,7 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
     });
 }
 
-// q = K32 p and p.q.  DIRECT: p as mx_update left it, gathered alone.  Otherwise
+// q = K32 p and p.q.  DIRECT: p as mx_update_staged left it, gathered alone.  Otherwise
 // p = z + beta p_old is formed on the fly from the (z, p_old) pairs and each row
 // writes its p.
 template <int STORAGE, bool DIRECT>
