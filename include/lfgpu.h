@@ -83,7 +83,9 @@ enum {
     LFGPU_OPTION_IC0_SWEEP = 1      /* LFGPU_IC0_SWEEP_*: how the IC(0) triangular sweeps are scheduled */
 };
 /* AUTO: by levels (one thread-block cluster walks the dependency levels) when the
- * pattern's level schedule fits the cluster's shared-memory ring, else POLLED.
+ * pattern's level schedule fits the cluster's shared-memory ring and its levels
+ * hold 192 rows or more on average, else POLLED.  The mixed-precision loop always
+ * sweeps by levels.
  * LEVELS: by levels, LFGPU_ERR_UNSUPPORTED where the schedule does not fit.
  * POLLED: row chunks in sweep order, each row polling for its operands (FP64 only). */
 enum { LFGPU_IC0_SWEEP_AUTO = 0, LFGPU_IC0_SWEEP_LEVELS = 1, LFGPU_IC0_SWEEP_POLLED = 2 };
