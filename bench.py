@@ -180,18 +180,18 @@ def spmv_bytes(kind: str, n: int, nnz: int, nblocks: int) -> int:
     return nblocks * (4 * s + 4) + 4 * (n // 2 + 1) + 2 * s * n
 
 
-def product_bytes(storage: str, n: int, matrix_bytes: int, precond: str = "jacobi") -> int:
+def product_bytes(n: int, matrix_bytes: int, precond: str = "jacobi") -> int:
     """Algorithmic bytes of one inner-loop product launch (mx_product): the FP32
-    matrix as the library streams it (values and column indices, int32 or 16-bit
-    block-column offsets; the solve report's matrix_bytes_per_matvec), the row
-    offsets and the FP32 diagonal pair (hi, lo) read once, q written once.  With
-    the pointwise preconditioners (Jacobi, 2x2 blocks) the update has formed p:
-    p is read once.  With the others the product forms p from z and the previous
-    p: both read once, p written once."""
+    matrix as the library streams it (2x2 blocks with int32 or 16-bit block-column
+    offsets, for BSR storage and for the paired CSR patterns of these meshes; the
+    solve report's matrix_bytes_per_matvec), the block-row offsets and the FP32
+    diagonal pair (hi, lo) read once, q written once.  With the pointwise
+    preconditioners (Jacobi, 2x2 blocks) the update has formed p: p is read once.
+    With the others the product forms p from z and the previous p: both read
+    once, p written once."""
     direct = precond in ("jacobi", "block")
     vectors = 4 * n * ((1 + 2 + 1) if direct else (2 + 2 + 2))
-    rows = n + 1 if storage == "csr" else n // 2 + 1
-    return matrix_bytes + 4 * rows + vectors
+    return matrix_bytes + 4 * (n // 2 + 1) + vectors
 
 
 # ---------------------------------------------------------------------- CPU leg
@@ -650,7 +650,7 @@ def run_ours(args) -> int:
                                     unrolled=args.roofline_passes), download=False)
     product_us = prof.phase_ms[0] * 1e3 / args.roofline_passes
     kernel_name = f"mx_product<{args.storage.upper()}>"
-    alg = product_bytes(args.storage, n, prof.matrix_bytes_per_matvec, args.precond)
+    alg = product_bytes(n, prof.matrix_bytes_per_matvec, args.precond)
     achieved = alg / (product_us * 1e-6) / 1e9
     traffic = profiled_traffic(kernel_name)
     roofline = {"bound": "hbm", "kernel": kernel_name, "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],

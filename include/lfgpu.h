@@ -129,8 +129,10 @@ typedef struct lfgpu_report {
     double matvec_ms;                /* device time of one standalone SpMV x matvec_calls */
     int64_t matvec_calls;
     int64_t matrix_bytes_per_matvec; /* bytes of the matrix one product streams (int32 columns; mixed BSR:
-                                        16-bit column offsets when they fit) */
-    double storage_convert_ms;
+                                        16-bit column offsets when they fit; mixed CSR of a paired
+                                        pattern: the BSR blocks, its FP32 working copy) */
+    double storage_convert_ms;       /* CSR -> BSR conversion this solve ran (BSR storage; mixed CSR of a
+                                        paired pattern) */
     double preconditioner_setup_ms;
     double preconditioner_apply_ms;  /* IC0 only: device time of the triangular sweeps */
     int64_t subdomains;              /* block / subdomain: number of subdomains (2x2 nodal blocks for block) */

@@ -693,10 +693,12 @@ int lfgpu_solve(lfgpu_t h, const lfgpu_solve_options* o, double* u_out, lfgpu_re
             r.fallback_fp64 = 1;
         }
         r.solve_ms = total_ms;
-        r.storage_convert_ms = (o->storage == LFGPU_STORAGE_BSR && !had_bsr) ? h->last_convert_ms : 0.0;
+        // The graph loop's FP32 copy of a paired CSR pattern is the BSR blocks.
+        const bool blocks = o->storage == LFGPU_STORAGE_BSR || (s.mixed && !o->persistent && h->paired);
+        r.storage_convert_ms = (blocks && !had_bsr && h->bsr_version == h->k_version) ? h->last_convert_ms : 0.0;
         r.matvec_calls = r.iterations + r.refinements;
         r.matrix_bytes_per_matvec =
-            o->storage == LFGPU_STORAGE_BSR
+            blocks
                 ? h->nblocks * (s.mixed ? 4 * 4 + (h->bcol16_ok ? 2 : 4) : 4 * 8 + 4)
                 : h->nnz * (s.mixed ? 4 + (h->col16_ok ? 2 : 4) : 8 + 4);
         // True residual ||f - K u|| in FP64.

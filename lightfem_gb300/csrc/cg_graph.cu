@@ -126,7 +126,7 @@ struct CgArgs {
     double target, reduction;
     long long maxit, max_ref;
     int restart;
-    int paired;    // rows 2i and 2i + 1 share one column list of (2j, 2j + 1) pairs (the CSR products take them as blocks)
+    int paired;    // CSR storage with a paired pattern: the mixed loop's FP32 copy is the BSR blocks
     int use_cond;  // 0 in the unrolled profiling graph, which has no conditional nodes
     int half;      // the body iteration (0 .. 7) whose IF handle `branch` is
     cudaGraphConditionalHandle loop, branch;
@@ -424,66 +424,6 @@ __device__ __forceinline__ void bsr32_rows(const CgArgs& a, const G& g, Out&& ou
                 const float4 v0 = ld_stream(a.bval32 + k);
                 const float4 v1 = t1 ? ld_stream(a.bval32 + k + 4) : zero;
                 const float4 v2 = t2 ? ld_stream(a.bval32 + k + 8) : zero;
-                const float2 x0 = g(c0), x1 = g(c1), x2 = g(c2);
-                s0 += v0.x * x0.x + v0.y * x0.y;
-                s1 += v0.z * x0.x + v0.w * x0.y;
-                s0 += v1.x * x1.x + v1.y * x1.y;
-                s1 += v1.z * x1.x + v1.w * x1.y;
-                s0 += v2.x * x2.x + v2.y * x2.y;
-                s1 += v2.z * x2.x + v2.w * x2.y;
-            }
-        }
-        s0 = quad_sum(s0);
-        s1 = quad_sum(s1);
-        if (act && sub == 0) out(node, make_float2(s0, s1));
-    }
-}
-
-// FP32 CSR rows of a paired pattern (rows 2i and 2i + 1 share one column list of
-// (2j, 2j + 1) pairs), taken two at a time as the 2x2 blocks of node i: the same
-// loop as bsr32_rows, with each block's top and bottom halves read from the two
-// rows' entries (8 bytes each) and one 8-byte gather per block instead of four
-// 4-byte ones.  The blocks hold the values the BSR product reads, in the same
-// order, so the result equals its bit for bit.
-__device__ __forceinline__ float2 ld_stream2(const float* p) { return __ldcs(reinterpret_cast<const float2*>(p)); }
-
-template <typename G, typename Out>
-__device__ __forceinline__ void csr32_pair_rows(const CgArgs& a, const G& g, Out&& out) {
-    const int lane = threadIdx.x & 31, sub = lane & 3;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int stride = ((gridDim.x * blockDim.x) >> 5) * 8;
-    int node = warp * 8 + (lane >> 2);
-    int nb_b = 0, nb_e = 0;
-    if (node < a.nb) {
-        nb_b = __ldg(a.rowptr + 2 * node);
-        nb_e = __ldg(a.rowptr + 2 * node + 1);
-    }
-    for (int base = warp * 8; base < a.nb; base += stride, node += stride) {  // warp-uniform
-        const bool act = node < a.nb;
-        const int b0 = nb_b, b1 = nb_e, e = (b1 - b0) / 2;  // block m: entries b0 + 2m (top), b1 + 2m (bottom)
-        if (node + stride < a.nb) {
-            nb_b = __ldg(a.rowptr + 2 * (node + stride));
-            nb_e = __ldg(a.rowptr + 2 * (node + stride) + 1);
-        }
-        float s0 = 0.f, s1 = 0.f;
-        if (act) {
-            // Columns as 16-bit offsets from row 2i when they fit; block column j = c / 2.
-            auto col = [&](int m) {
-                return a.col16 ? node + (ld_stream(a.col16 + b0 + 2 * m) >> 1) : (ld_stream(a.col + b0 + 2 * m) >> 1);
-            };
-            auto val = [&](int m) {
-                const float2 t = ld_stream2(a.K32 + b0 + 2 * m), u = ld_stream2(a.K32 + b1 + 2 * m);
-                return make_float4(t.x, t.y, u.x, u.y);
-            };
-            for (int k = sub; k < e; k += 12) {
-                const bool t1 = k + 4 < e, t2 = k + 8 < e;
-                const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-                const int c0 = col(k);
-                const int c1 = t1 ? col(k + 4) : c0;
-                const int c2 = t2 ? col(k + 8) : c0;
-                const float4 v0 = val(k);
-                const float4 v1 = t1 ? val(k + 4) : zero;
-                const float4 v2 = t2 ? val(k + 8) : zero;
                 const float2 x0 = g(c0), x1 = g(c1), x2 = g(c2);
                 s0 += v0.x * x0.x + v0.y * x0.y;
                 s1 += v0.z * x0.x + v0.w * x0.y;
@@ -831,14 +771,15 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
 
 // q = K32 p and p.q.  DIRECT: p as mx_update_staged left it, gathered alone.  Otherwise
 // p = z + beta p_old is formed on the fly from the (z, p_old) pairs and each row
-// writes its p.
+// writes its p.  The FP32 copy of K is the BSR blocks for BSR storage and for a
+// paired CSR pattern (a.paired), FP32 CSR rows otherwise.
 template <int STORAGE, bool DIRECT>
 __global__ void __launch_bounds__(kThreads, 8) mx_product(CgArgs a) {  // 8 CTAs an SM: the grid in one wave
     if (a.st->done) return;
     const float beta = a.st->beta32;
     const float4* zp4 = zp_buffer(a, a.st->it);
     FloatPair acc;
-    // Gathers and row results per node (a 2x2 block row, or a pair of CSR rows).
+    // Gathers and row results per node (a 2x2 block row).
     const float2* hi2 = reinterpret_cast<const float2*>(a.dhi);
     const float2* lo2 = reinterpret_cast<const float2*>(a.dlo);
     const float2* p2 = reinterpret_cast<const float2*>(a.p32);
@@ -864,9 +805,7 @@ __global__ void __launch_bounds__(kThreads, 8) mx_product(CgArgs a) {  // 8 CTAs
         reinterpret_cast<float2*>(a.q32)[node] = y;
         acc.add(pn.x * y.x + pn.y * y.y);
     };
-    if (STORAGE == LFGPU_STORAGE_CSR && a.paired) {
-        csr32_pair_rows(a, gather_node, finish_node);
-    } else if (STORAGE == LFGPU_STORAGE_CSR) {
+    if (STORAGE == LFGPU_STORAGE_CSR && !a.paired) {
         const float2* zp2 = reinterpret_cast<const float2*>(zp4);
         const float* p = a.p32;
         csr32_rows(a,
@@ -2419,15 +2358,23 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
         c.xlo.ensure(n);
         a.xhi = c.xhi;
         a.xlo = c.xlo;
-        if (s.storage == LFGPU_STORAGE_BSR) {
+        if (s.storage == LFGPU_STORAGE_BSR || c.paired) {
+            // A paired CSR pattern (rows 2i and 2i + 1 share one column list of
+            // (2j, 2j + 1) pairs, as every Q4 and bar pattern does) holds the same
+            // entries as the BSR form, so its FP32 working copy is the BSR blocks:
+            // the FP32 product is the BSR one, bit for bit, while the FP64 products
+            // of the refinement keep the CSR storage.  One float4 a block and a
+            // 16-bit offset replace 8 bytes of values and the column pair.
             ensure_bsr32(c);
+            a.brow = c.brow;
+            a.bcol = c.bcol;
             a.bval32 = reinterpret_cast<const float4*>(c.bval32.p);
             a.bcol16 = c.bcol16_ok ? c.bcol16.p : nullptr;
+            a.paired = s.storage == LFGPU_STORAGE_CSR ? 1 : 0;
         } else {
             ensure_csr32(c);
             a.K32 = c.K32;
             a.col16 = c.col16_ok ? c.col16.p : nullptr;
-            a.paired = c.paired ? 1 : 0;
         }
         a.dhi = c.diag_hi;
         a.dlo = c.diag_lo;
