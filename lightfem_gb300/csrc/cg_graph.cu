@@ -12,7 +12,9 @@
 // from the device (cudaGraphSetConditional) by the block that finishes each
 // reduction.  Scalars (rho, alpha, beta, norms, counters) live in a device
 // CgState.  Dot products are reduced deterministically: every block publishes
-// its partial, and the last block to arrive adds them in block order.
+// its partial, and the last block to arrive adds them in a fixed order.  The
+// mixed loop's direct form has no last block in its product: every CTA of the
+// update that follows adds the product's partials itself, in that same order.
 //
 // Products: a quarter warp per CSR row or per BSR block row, several entries or
 // blocks in flight per lane (FP64 BSR: a whole 2x2 block per lane as two 16-byte
@@ -115,6 +117,7 @@ struct CgArgs {
         int levels;
     } sw[2];
     int staged_stash;              // mx_update_staged: nodes per CTA whose (z, p) stay in shared memory
+    int product_grid;              // CTAs of mx_product (the direct form's update adds their p.q pairs)
     int sw_window;                 // ring slots per CTA (a power of two)
     int sw_maxp, sw_maxe;          // the largest piece: positions, entries (the stage size)
     void* sw_y;                    // forward result in backward positions (double or float)
@@ -212,7 +215,16 @@ struct FloatPair {
 // sums as pairs, then the warps' pairs in warp 0, whose threads all get the CTA's
 // totals as pairs in w (the other threads' w is zero).  FP32 arithmetic only: on
 // GB300 a dependent FP64 add takes about as long as a dozen FP32 ones.
-template <int K>
+// NT > 0: only the CTA's first NT threads take part, synchronised on named barrier 1.
+template <int NT>
+__device__ __forceinline__ void pair_reduce_sync() {
+    if constexpr (NT == 0)
+        __syncthreads();
+    else
+        asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
+}
+
+template <int K, int NT = 0>
 __device__ __forceinline__ void block_pair_reduce(FloatPair (&v)[K], FloatPair (&w)[K]) {
     __shared__ float2 s_warp[32 * kMaxReduce];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -230,11 +242,11 @@ __device__ __forceinline__ void block_pair_reduce(FloatPair (&v)[K], FloatPair (
 #pragma unroll
         for (int k = 0; k < K; ++k) s_warp[warp * K + k] = make_float2(v[k].hi, v[k].lo);
     }
-    __syncthreads();
+    pair_reduce_sync<NT>();
 #pragma unroll
     for (int k = 0; k < K; ++k) w[k] = FloatPair{};
     if (warp == 0) {
-        const int nw = blockDim.x >> 5;
+        const int nw = (NT == 0 ? static_cast<int>(blockDim.x) : NT) >> 5;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             if (lane < nw) {
@@ -251,7 +263,7 @@ __device__ __forceinline__ void block_pair_reduce(FloatPair (&v)[K], FloatPair (
             }
         }
     }
-    __syncthreads();  // s_warp is free again
+    pair_reduce_sync<NT>();  // s_warp is free again
 }
 
 // The grid-wide step for FP32-pair values: each CTA leaves its pair totals, and
@@ -769,10 +781,13 @@ __global__ void __launch_bounds__(kThreads) mx_init(CgArgs a) {
     });
 }
 
-// q = K32 p and p.q.  DIRECT: p as mx_update_staged left it, gathered alone.  Otherwise
-// p = z + beta p_old is formed on the fly from the (z, p_old) pairs and each row
-// writes its p.  The FP32 copy of K is the BSR blocks for BSR storage and for a
-// paired CSR pattern (a.paired), FP32 CSR rows otherwise.
+// q = K32 p and p.q.  DIRECT: p as mx_update_staged left it, gathered alone, and
+// each CTA only leaves its p.q pair: the update's CTAs form alpha from them, so no
+// CTA of the product waits at the end for a last one's sum and division.
+// Otherwise p = z + beta p_old is formed on the fly from the (z, p_old) pairs, each
+// row writes its p, and the last CTA sets alpha.  The FP32 copy of K is the BSR
+// blocks for BSR storage and for a paired CSR pattern (a.paired), FP32 CSR rows
+// otherwise.
 template <int STORAGE, bool DIRECT>
 __global__ void __launch_bounds__(kThreads, 8) mx_product(CgArgs a) {  // 8 CTAs an SM: the grid in one wave
     if (a.st->done) return;
@@ -834,6 +849,15 @@ __global__ void __launch_bounds__(kThreads, 8) mx_product(CgArgs a) {  // 8 CTAs
         bsr32_rows(a, gather_node, finish_node);
     }
     FloatPair v[1] = {acc};
+    if constexpr (DIRECT) {
+        // Each CTA leaves its p.q pair; every CTA of mx_update_staged adds them for alpha.
+        FloatPair w[1];
+        block_pair_reduce<1>(v, w);
+        if (threadIdx.x == 0)
+            reinterpret_cast<float2*>(a.partials + static_cast<size_t>(a.blocks) * kMaxReduce)[blockIdx.x * kMaxReduce] =
+                make_float2(w[0].hi, w[0].lo);
+        return;
+    }
     reduce_last<1>(a, 1, v, [&](const double* t) {
         CgState* s = a.st;
         if (!(t[0] > 0.0) || !isfinite(t[0])) {
@@ -1763,6 +1787,12 @@ __global__ void __launch_bounds__(kThreads) precond_apply_kernel(CgArgs a) {
 // ms with six stages).  The arithmetic per node is mx_update's, in the same order.
 // (z, p) of the CTA's first staged_stash nodes stay in shared memory for the
 // direction pass; any further ones read r, p and the preconditioner again from L2.
+// alpha: while the producer fills the first stages, the consumers of every CTA add
+// the product's CTA pairs of p.q (the order and arithmetic of reduce_tail_pair,
+// so alpha is the same in every CTA and the same as a last CTA of the product
+// would set) and divide.  That moved the 1000x1000 BSR/Jacobi solve from 1,000 to
+// 947 ms on one GB300, same iterations: the product's last CTA had held up the
+// end of every product launch.
 constexpr int kStagedThreads = 256;  // consumers: one node per thread and chunk
 constexpr int kStagedChunk = kStagedThreads;
 constexpr int kStagedBlock = kStagedThreads + 32;  // plus the producer warp
@@ -1795,7 +1825,8 @@ __global__ void __launch_bounds__(kStagedBlock) mx_update_staged(CgArgs a) {
         return;
     }
     const unsigned go0 = a.st->go;  // moves only after every CTA has arrived
-    const float alpha = a.st->alpha32, alpha_lo = a.st->alpha32_lo;
+    __shared__ float s_alpha[2];
+    __shared__ int s_bad;
     const int tid = threadIdx.x;
     const int per = staged_per_cta(a.nb, gridDim.x);
     const int n0 = min(a.nb, static_cast<int>(blockIdx.x) * per), n1 = min(a.nb, n0 + per);
@@ -1827,6 +1858,45 @@ __global__ void __launch_bounds__(kStagedBlock) mx_update_staged(CgArgs a) {
     const unsigned long long limit = a.status->wait_limit_ns;
     bool ok = true;
     FloatPair rr, rz;
+    float alpha = 0.f, alpha_lo = 0.f;
+    bool bad = false;
+    if (tid < kStagedThreads) {
+        // alpha = rho / p.q from mx_product's CTA pairs, while the producer fills the
+        // first stages.  Every CTA adds them in the same order with the same
+        // arithmetic, so all CTAs hold the same alpha.
+        const float2* part = reinterpret_cast<const float2*>(a.partials + static_cast<size_t>(a.blocks) * kMaxReduce);
+        FloatPair acc[1];
+        for (int b = tid; b < a.product_grid; b += kStagedThreads) {
+            const float2 t = __ldcg(part + b * kMaxReduce);
+            acc[0].add(FloatPair{t.x, t.y});
+        }
+        FloatPair tot[1];
+        block_pair_reduce<1, kStagedThreads>(acc, tot);
+        if (tid == 0) {
+            const double pq = static_cast<double>(tot[0].hi) + static_cast<double>(tot[0].lo);
+            s_bad = !(pq > 0.0) || !isfinite(pq);
+            float hi = 0.f, lo = 0.f;
+            if (!s_bad) pair_quotient(a.st->rho, pq, hi, lo);
+            s_alpha[0] = hi;
+            s_alpha[1] = lo;
+            if (blockIdx.x == 0) {
+                if (s_bad) {
+                    a.st->status = LFGPU_ERR_NOT_SPD;
+                    a.st->done = 1;
+                    set_branch(a, false);
+                    set_loop(a, false);
+                } else {
+                    a.st->alpha32 = hi;
+                    a.st->alpha32_lo = lo;
+                    a.st->alpha = static_cast<double>(hi) + static_cast<double>(lo);
+                }
+            }
+        }
+        pair_reduce_sync<kStagedThreads>();
+        alpha = s_alpha[0];
+        alpha_lo = s_alpha[1];
+        bad = s_bad != 0;
+    }
     if (tid >= kStagedThreads) {
         // Producer warp: lane 0 refills a stage as soon as every consumer warp is done with it.
         if (tid == kStagedThreads) {
@@ -1842,7 +1912,7 @@ __global__ void __launch_bounds__(kStagedBlock) mx_update_staged(CgArgs a) {
         ok = mbar_wait(full + s, static_cast<unsigned>(k / S) & 1u, a.status, limit) && ok;
         const unsigned char* st = staged_smem + s * SB;
         const int i = n0 + k * C + tid;
-        if (i < n1) {
+        if (i < n1 && !bad) {
             const float2 pv = reinterpret_cast<const float2*>(st)[tid];
             const float2 qv = reinterpret_cast<const float2*>(st + C * 8)[tid];
             float2 hv = reinterpret_cast<const float2*>(st + 2 * C * 8)[tid];
@@ -1881,6 +1951,7 @@ __global__ void __launch_bounds__(kStagedBlock) mx_update_staged(CgArgs a) {
         __syncthreads();
         return;
     }
+    if (s_bad) return;  // p.q not positive: the solve ends (block 0 set the status); every copy has landed
     FloatPair v[2] = {rr, rz};
     const bool last = reduce_last<2>(a, 2, v, [&](const double* t) { update_totals<false>(a, t); });
     if (!wait_for_beta(a, last, go0)) return;
@@ -2398,6 +2469,7 @@ PcgResult run_cg_graph(Context& c, const SolveSetup& s, float* kernel_ms) {
     c.partials.ensure(static_cast<size_t>(kSlots) * kMaxReduce * reducing);
     a.partials = c.partials;
     a.blocks = reducing;
+    a.product_grid = blocks;
     c.cg_state.ensure(sizeof(CgState));
     a.st = reinterpret_cast<CgState*>(c.cg_state.p);
     a.status = c.status;
