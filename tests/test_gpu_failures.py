@@ -88,3 +88,32 @@ def test_assembly_failure_message(native, golden_json, name):
     with pytest.raises(RuntimeError) as err:
         LinearElasticSolver().solve(indexed(ASSEMBLY_FAILURES[name]()))
     assert str(err.value) == assembly_failure_message(golden_json, name)
+
+
+@pytest.mark.parametrize("precond", ["jacobi", "block"])
+def test_mixed_direct_form_indefinite(native, precond):
+    """Above 300,000 nodes the mixed loop runs in its direct form, where every CTA
+    of the update forms alpha from the product's per-CTA p.q pairs and the update
+    makes pcg_solve's curvature check (src/solver.cpp:591-593).  On the 1000x1000
+    cantilever with one element's modulus at -10x the others (an indefinite K)
+    the solve must end with one of pcg_solve's errors, not run on or stall."""
+    from lightfem_gb300 import mesh
+    from lightfem_gb300.solver import upload_model
+
+    m = mesh.workload(2)
+    ne = m.element_ids.shape[0]
+    young = np.full(ne, 70.0e9)
+    young[ne // 2 + 500] = -7.0e11
+    m.material_ids = np.arange(1, ne + 1)
+    m.young, m.poisson, m.thickness = young, np.full(ne, 0.33), np.full(ne, 0.01)
+    m.element_material = np.arange(1, ne + 1)
+    m.sort_and_index()
+    m.index_with_node_order(native.host_rcm(m.node_ids, m.element_nodes))
+    ctx = native.Context(0)
+    upload_model(ctx, m)
+    ctx.assemble("coloring")
+    ctx.apply_dirichlet()
+    with pytest.raises(native.GpuError) as err:
+        ctx.solve(ctx.options(1e-8, 200000, "bsr", precond, "mixed"), download=False)
+    assert err.value.code in (native.ERR_NOT_SPD, native.ERR_RHO), str(err.value)
+    ctx.close()
