@@ -107,7 +107,7 @@ int guarded(lfgpu_t h, F&& f) {
     }
 }
 
-void install_colors(Context& c, const int* colors);
+void install_colors(Context& c, const int* colors, bool check = true);
 void install_finish(Context& c);
 
 // Host copies the map/colour validation needs; set on lfgpu_set_pattern.
@@ -167,8 +167,9 @@ void install_pattern(Context& c, i64 n, i64 nnz, const int64_t* rowptr64, const 
     install_finish(c);
 }
 
-// Colours: per-colour element lists; no two elements of a colour may share a node.
-void install_colors(Context& c, const int* colors) {
+// Colours: per-colour element lists; no two elements of a colour may share a node
+// (checked unless the library coloured the mesh itself: check = false).
+void install_colors(Context& c, const int* colors, bool check) {
     const int* en = c.h_elem_nodes.data();
     c.n_colors = 0;
     c.color_offsets.assign(1, 0);
@@ -186,8 +187,8 @@ void install_colors(Context& c, const int* colors) {
         order.resize(static_cast<size_t>(c.n_elem));
         std::vector<int> fill(c.color_offsets.begin(), c.color_offsets.end() - 1);
         for (i64 e = 0; e < c.n_elem; ++e) order[fill[colors[e]]++] = static_cast<int>(e);
-        std::vector<int> owner(static_cast<size_t>(c.n_nodes), -1);
-        for (int k = 0; k < c.n_colors; ++k)
+        std::vector<int> owner(check ? static_cast<size_t>(c.n_nodes) : 0, -1);
+        for (int k = 0; check && k < c.n_colors; ++k)
             for (int s = c.color_offsets[k]; s < c.color_offsets[k + 1]; ++s)
                 for (int a = 0; a < 4; ++a) {
                     const int nd = en[4 * static_cast<i64>(order[s]) + a];
@@ -419,7 +420,7 @@ int lfgpu_build_pattern(lfgpu_t h) {
         colouring.join();
         if (colouring_error) std::rethrow_exception(colouring_error);
         if (on_device) {
-            install_colors(*h, colors.data());
+            install_colors(*h, colors.data(), false);  // first fit: race-free by construction
             install_finish(*h);
         } else {  // a node with more elements than the device build handles
             const HostPattern p = build_pattern(h->n_nodes, h->n_elem, h->h_elem_nodes.data());
