@@ -1340,7 +1340,7 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
     __shared__ __align__(8) unsigned long long full[S], empty[S], ringbar[SR];
     __shared__ int4 piece_of[S];
     __shared__ int rearm_of[S];
-    __shared__ int s_failed;
+    __shared__ int s_failed, s_issued;
     const CgArgs::SweepPlan& sp = a.sw[kFwd ? 0 : 1];
     const int levels = sp.levels;
     const int mask = a.sw_window - 1;
@@ -1355,6 +1355,7 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
     };
     if (tid == 0) {
         s_failed = 0;
+        s_issued = 0;
         for (int s = 0; s < S; ++s) {
             mbar_init(full + s, 1);
             mbar_init(empty + s, 1);
@@ -1386,6 +1387,7 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
         };
         int4 cur_pc, next_pc;
         int cur_rearm, next_rearm;
+        int issued = 0;  // levels whose copies lane 0 issued
         batch(0, cur_pc, cur_rearm);
         batch(32, next_pc, next_rearm);
         for (int L = 0; L < levels; ++L) {
@@ -1401,10 +1403,13 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
             pc.z = __shfl_sync(0xffffffffu, cur_pc.z, i);
             pc.w = __shfl_sync(0xffffffffu, cur_pc.w, i);
             const int rearm = __shfl_sync(0xffffffffu, cur_rearm, i);
-            if (lane == 0) {
-                const int s = L % S;
-                // The stage is free once the consumers are done with level L - S.
-                if (L >= S) ok = wait_phase(empty + s, static_cast<unsigned>(L / S - 1) & 1u, a.status, L) && ok;
+            const int s = L % S;
+            // The stage is free once the consumers are done with level L - S.  After
+            // a wait that ran out nothing more is issued, so a stage never holds more
+            // than one outstanding set of copies (no phase gets a second arrival).
+            if (lane == 0 && ok && L >= S) ok = wait_phase(empty + s, static_cast<unsigned>(L / S - 1) & 1u, a.status, L);
+            if (lane == 0 && ok) {
+                issued = L + 1;
                 piece_of[s] = pc;
                 rearm_of[s] = rearm;
                 unsigned char* st = stages + static_cast<size_t>(s) * lay.bytes;
@@ -1435,6 +1440,7 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
             }
             __syncwarp();
         }
+        if (lane == 0) s_issued = issued;
     } else {
         // ---- consumers: one row per thread and pass.
         unsigned ring_at[kSweepCluster], bar_at[kSweepCluster];
@@ -1477,7 +1483,9 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
             };
             // This thread's first row: its operands come out of the stage before the
             // wait for level L - 1, so only the ring reads and the arithmetic follow it.
-            const bool have = tid < cnt;
+            // A thread whose wait ran out reads nothing of the stage, which may not
+            // have arrived, and publishes nothing.
+            const bool have = ok && tid < cnt;
             int4 d = make_int4(0, 0, 0, 0);
             T rhs = T(0), inv = T(0), rr = T(0);
             int dk[kSweepUnroll];
@@ -1499,7 +1507,7 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
                 const int prev = L - 1;
                 ok = wait_phase(ringbar + prev % SR, static_cast<unsigned>(prev / SR) & 1u, a.status, prev) && ok;
             }
-            if (have) {
+            if (have && ok) {
                 T acc = rhs;
                 T prod[kSweepUnroll];
 #pragma unroll
@@ -1513,7 +1521,7 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
                 publish(pc.x + tid, d, sweep_mul(acc, inv), rr);
             }
             // Pieces wider than the consumer threads: further rows, read after the wait.
-            for (int t = tid + kSweepConsumers; t < cnt; t += kSweepConsumers) {
+            for (int t = tid + kSweepConsumers; ok && t < cnt; t += kSweepConsumers) {
                 const int p = pc.x + t;
                 const int4 e = sdesc[t];
                 T acc = srhs[p - pos0];
@@ -1522,7 +1530,7 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
                 publish(p, e, sweep_mul(acc, sinv[p - pos0]), MODE == 3 ? srr[p - pos0] : T(0));
             }
             consumers_sync();  // every consumer is done with stage s and has seen level L - 1 arrive
-            if (tid == 0) {
+            if (tid == 0 && ok) {  // after a wait that ran out: no arrival on a phase that may be pending
                 // The ring mbarrier of level L - 1 is free again: armed for level
                 // L - 1 + SR, whose width the piece table carries with level L.
                 const int rearm = rearm_of[s];
@@ -1550,6 +1558,13 @@ __global__ void __cluster_dims__(kSweepCluster, 1, 1) __launch_bounds__(kSweepBl
             a.st->status = LFGPU_ERR_TIMEOUT;
             a.st->done = 1;
             set_loop(a, false);
+            // This CTA's own copies: at most one outstanding set per stage, the last
+            // level issued into it, waited for with a bound the abort does not cut.
+            const int issued = s_issued;
+            for (int st = 0; st < S && st < issued; ++st) {
+                const int last = st + ((issued - 1 - st) / S) * S;
+                mbar_drain(full + st, static_cast<unsigned>(last / S) & 1u);
+            }
             const unsigned long long t0 = global_ns();
             while (global_ns() - t0 < 100000ull) {
             }
@@ -1814,12 +1829,12 @@ constexpr int staged_stage_bytes() {  // p, q, hi, lo, r (8 bytes a node each) a
 inline __host__ __device__ int staged_per_cta(int nb, int grid) { return ((nb + grid - 1) / grid + 3) & ~3; }
 
 template <int PRECOND>
-__global__ void __launch_bounds__(kStagedBlock) mx_update_staged(CgArgs a) {
+__global__ void __launch_bounds__(kStagedBlock, kStagedCtasPerSm) mx_update_staged(CgArgs a) {
     constexpr int C = kStagedChunk, S = kStagedStages, PCB = staged_pc_bytes<PRECOND>();
     constexpr int SB = staged_stage_bytes<PRECOND>();
     extern __shared__ __align__(128) unsigned char staged_smem[];
     __shared__ __align__(8) unsigned long long full[S], empty[S];
-    __shared__ int s_failed;
+    __shared__ int s_failed, s_issued;
     if (a.st->done) {
         if (blockIdx.x == 0 && threadIdx.x == 0) set_branch(a, false);
         return;
@@ -1848,6 +1863,7 @@ __global__ void __launch_bounds__(kStagedBlock) mx_update_staged(CgArgs a) {
     };
     if (tid == 0) {
         s_failed = 0;
+        s_issued = 0;
         for (int s = 0; s < S; ++s) {
             mbar_init(full + s, 1);
             mbar_init(empty + s, kStagedWarps);
@@ -1898,18 +1914,31 @@ __global__ void __launch_bounds__(kStagedBlock) mx_update_staged(CgArgs a) {
         bad = s_bad != 0;
     }
     if (tid >= kStagedThreads) {
-        // Producer warp: lane 0 refills a stage as soon as every consumer warp is done with it.
+        // Producer warp: lane 0 refills a stage as soon as every consumer warp is done
+        // with it.  If that wait runs out it issues nothing more, so a stage never
+        // holds more than one outstanding set of copies: no full-barrier phase gets a
+        // second arrival, and no copy lands on data still being read.
         if (tid == kStagedThreads) {
-            for (int k = 0; k < chunks; ++k) {
+            int k = 0;
+            for (; k < chunks; ++k) {
                 const int s = k % S;
-                if (k >= S) ok = mbar_wait(empty + s, static_cast<unsigned>(k / S - 1) & 1u, a.status, limit) && ok;
+                if (k >= S && !mbar_wait(empty + s, static_cast<unsigned>(k / S - 1) & 1u, a.status, limit)) {
+                    ok = false;
+                    break;
+                }
                 issue(k);
             }
+            s_issued = k;
         }
     } else {
     for (int k = 0; k < chunks; ++k) {
         const int s = k % S;
-        ok = mbar_wait(full + s, static_cast<unsigned>(k / S) & 1u, a.status, limit) && ok;
+        // A warp goes on only if every lane saw the stage arrive; after a wait that
+        // ran out it neither reads nor releases another stage.
+        if (!__all_sync(0xffffffffu, mbar_wait(full + s, static_cast<unsigned>(k / S) & 1u, a.status, limit))) {
+            ok = false;
+            break;
+        }
         const unsigned char* st = staged_smem + s * SB;
         const int i = n0 + k * C + tid;
         if (i < n1 && !bad) {
@@ -1937,15 +1966,18 @@ __global__ void __launch_bounds__(kStagedBlock) mx_update_staged(CgArgs a) {
     if (!ok) s_failed = 1;
     __syncthreads();
     if (s_failed) {
-        // A copy did not arrive in time: end the solve (the status word says why),
-        // and give copies still on their way into this CTA's stages time to land
-        // before its shared memory is released.
+        // A wait ran out: end the solve (the status word says why).  Copies this CTA
+        // issued land before its shared memory is released: each stage has at most
+        // one outstanding set, its last chunk's, whose full phase is waited for with
+        // a fixed bound that the abort flag does not cut short.
         if (tid == 0) {
             a.st->done = 1;
             set_branch(a, false);
             set_loop(a, false);
-            const unsigned long long t0 = global_ns();
-            while (global_ns() - t0 < 100000ull) {
+            const int issued = s_issued;
+            for (int st = 0; st < S && st < issued; ++st) {
+                const int last = st + ((issued - 1 - st) / S) * S;  // the last chunk issued into stage st
+                mbar_drain(full + st, static_cast<unsigned>(last / S) & 1u);
             }
         }
         __syncthreads();

@@ -489,6 +489,18 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
     return true;
 }
 
+// Wait for copies this CTA already issued into a stage to land before it releases
+// its shared memory, after another wait ran out: a bounded spin on the stage's
+// phase that neither the abort flag nor the handle's wait limit cuts short (a copy
+// lands within microseconds).  False if even this bound ran out.
+constexpr unsigned long long kDrainNs = 10000000ull;
+__device__ __forceinline__ bool mbar_drain(unsigned long long* bar, unsigned parity) {
+    const unsigned long long start = global_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (global_ns() - start > kDrainNs) return false;
+    return true;
+}
+
 inline int grid_for(i64 work, int block, int cap = 1 << 20) {
     i64 g = (work + block - 1) / block;
     if (g < 1) g = 1;

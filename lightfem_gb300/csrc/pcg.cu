@@ -202,11 +202,12 @@ __device__ __forceinline__ bool product(const TileSet& m, Pipe& pipe, DeviceStat
         const int s = gidx % kStages;
         const bool ok = mbar_wait(pipe.full + s, (gidx / kStages) & 1u, status, kCopyWaitNs);
         if (!__syncthreads_and(ok)) {
-            // Let the copies already in flight land before the CTA gives up.
+            // Let the copies already in flight land before the CTA gives up: this
+            // tile's, whose wait ran out, and the ones issued ahead of it.
             if (threadIdx.x == 0) {
-                for (int k = j + 1; k < nt && k < j + kStages; ++k) {
+                for (int k = j; k < nt && k < j + kStages; ++k) {
                     const unsigned gk = pipe.count + k;
-                    mbar_wait(pipe.full + gk % kStages, (gk / kStages) & 1u, status, kCopyWaitNs);
+                    mbar_drain(pipe.full + gk % kStages, (gk / kStages) & 1u);
                 }
             }
             __syncthreads();
