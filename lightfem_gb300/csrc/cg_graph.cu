@@ -724,14 +724,15 @@ constexpr bool applied_separately() {
 // nodes.  The product then gathers p alone, 8 bytes a node instead of the
 // (z, p_old) pair's 16, and writes no p.  p is the same fma of the same values as
 // when the product forms it, once per node instead of once per gather.  The wait
-// costs a few microseconds whatever the size, the saving grows with it.  Per
-// iteration of the mixed BSR/Jacobi solve on GB300 (n x n plane-strain
-// cantilevers, RCM), direct against (z, p_old) form: 400x400 (160,801 nodes)
-// 27.05 against 26.93 us; 500x500 (251,001) 31.17 against 30.98; 600x600
-// (361,201) 35.77 against 36.02; 700x700 (491,401) 41.90 against 42.11; 800x800
-// (641,601) 47.69 against 50.66.  The separately applied preconditioners keep
-// the (z, p_old) form: their z arrives after mx_update.
-constexpr long long kDirectMinNodes = 300000;
+// costs a few microseconds whatever the size, the saving grows with it, and the
+// direct form's update also forms alpha, so its product has no last-CTA tail.
+// Per iteration of the mixed BSR/Jacobi solve on GB300 (n x n plane-strain
+// cantilevers, RCM), direct against (z, p_old) form, one box: 400x400 (160,801
+// nodes) 22.92 against 25.23 us; 500x500 (251,001) 26.20 against 29.17.  (Before
+// the update formed alpha: 27.05 against 26.93 at 400x400, 47.69 against 50.66
+// at 800x800.)  Smaller meshes keep the (z, p_old) form until measured.  The
+// separately applied preconditioners keep it too: their z arrives after mx_update.
+constexpr long long kDirectMinNodes = 150000;
 
 bool direct_form(int precond, long long nodes) {
     return (precond == LFGPU_PRECOND_JACOBI || precond == LFGPU_PRECOND_BLOCK2) && nodes >= kDirectMinNodes;

@@ -92,7 +92,7 @@ def test_assembly_failure_message(native, golden_json, name):
 
 @pytest.mark.parametrize("precond", ["jacobi", "block"])
 def test_mixed_direct_form_indefinite(native, precond):
-    """Above 300,000 nodes the mixed loop runs in its direct form, where every CTA
+    """From 150,000 nodes on the mixed loop runs in its direct form, where every CTA
     of the update forms alpha from the product's per-CTA p.q pairs and the update
     makes pcg_solve's curvature check (src/solver.cpp:591-593).  On the 1000x1000
     cantilever with one element's modulus at -10x the others (an indefinite K)

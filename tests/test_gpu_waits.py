@@ -85,7 +85,7 @@ def test_persistent_grid_barrier_expires(native, golden_json):
 
 def test_mixed_update_direction_wait_expires(native, golden_json):
     """The mixed loop's update in its direct form (a pointwise preconditioner on a
-    mesh of 300,000 nodes or more): its CTAs wait for the last one's beta before
+    mesh of 150,000 nodes or more): its CTAs wait for the last one's beta before
     they form the next direction; with a 1 ns limit the first CTA to wait gives up
     and the solve ends."""
     model, ctx = _system(native, mesh.workload(2))  # 1000x1000, 1,002,001 nodes
